@@ -1,0 +1,189 @@
+/*
+ * rp.h — C ABI of the GB300 DEM step (librp.so).
+ *
+ * The reference exposes its engine only through a pyo3 extension module,
+ * `rusty_particles` (src/lib.rs:24-35), whose class `Simulation`
+ * (src/lib.rs:41-277) owns a Rust `simulation::Simulation`
+ * (src/simulation.rs:16-51). This header is the flat C boundary a binding
+ * (ctypes, cgo, a Rust `extern "C"` block, JNI) calls in its place. Every
+ * entry point below names the reference interface it replaces.
+ *
+ * Conventions
+ *   - Plain pointers and sizes only; no CUDA or torch types cross the ABI.
+ *   - Return codes: RP_OK (0) or a negative RP_E_* code. rp_last_error()
+ *     returns the message of the last failure on the calling thread.
+ *   - A handle is owned by one host thread at a time (like the reference's
+ *     `&mut self` methods); distinct handles are independent.
+ *   - Particle ids are indices in insertion order after removals, exactly as
+ *     the reference re-indexes (src/simulation.rs:216-219).
+ *   - All stepping runs on the GPU. There is no CPU fallback: without a
+ *     usable CUDA device, rp_enable_gpu / rp_step / rp_run fail with RP_E_CUDA.
+ */
+#ifndef RP_H
+#define RP_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RP_OK 0
+#define RP_E_INVALID_ARG (-1) /* maps to Python ValueError */
+#define RP_E_INDEX (-2)       /* maps to Python IndexError */
+#define RP_E_IO (-3)          /* maps to Python IOError */
+#define RP_E_CUDA (-4)        /* maps to Python RuntimeError */
+#define RP_E_DEVICE_FLAG (-5) /* device reported a condition it could not recover from */
+#define RP_E_TIMEOUT (-6)     /* a bounded device-side wait ran out */
+#define RP_E_NOMEM (-7)       /* host or device allocation failed */
+
+/* Normal force models, in the reference enum order (src/physics.rs:6-17). */
+#define RP_NORMAL_LINEAR 0
+#define RP_NORMAL_HERTZ 1
+#define RP_NORMAL_HYSTERETIC 2
+#define RP_NORMAL_JKR 3
+#define RP_NORMAL_SJKR 4
+/* Tangential force models, in the reference enum order (src/physics.rs:21-28). */
+#define RP_TANGENTIAL_COULOMB 0
+#define RP_TANGENTIAL_LINEAR_SPRING 1
+#define RP_TANGENTIAL_MINDLIN 2
+
+/* Arithmetic of the pair forces. State, accumulation and the integrator are
+ * FP64 in both modes. */
+#define RP_PREC_FP64 0  /* all pair math in FP64 */
+#define RP_PREC_MIXED 1 /* pair math in FP32 on FP64-differenced inputs */
+
+/* Interaction rules. */
+#define RP_MODE_PARITY 0   /* the reference's rules, including its defects */
+#define RP_MODE_PHYSICAL 1 /* minimum-image pairs once each, Mindlin G*, history per pair */
+
+typedef struct rp_sim rp_sim;
+
+/* Host-side state view used by rp_read_state / rp_write_state. Arrays are in
+ * particle-id order; vectors hold 3 doubles per particle. Any pointer may be
+ * NULL (that field is skipped). rp_write_state ignores n_particles. */
+typedef struct rp_state {
+  size_t n_particles;
+  double* position;         /* 3N */
+  double* velocity;         /* 3N */
+  double* angular_velocity; /* 3N */
+  double* acceleration;     /* 3N */
+  double* torque;           /* 3N */
+  double* position_residual;
+  double* velocity_residual;
+  double* angular_velocity_residual;
+  double* radius;  /* N */
+  double* mass;    /* N */
+  uint8_t* fixed;  /* N */
+} rp_state;
+
+typedef struct rp_stats {
+  uint64_t steps;              /* steps completed on this handle */
+  uint64_t particles;          /* current particle count */
+  uint64_t removed;            /* particles removed by the out-of-bounds rule */
+  uint64_t neighbor_rebuilds;  /* Verlet-list rebuilds */
+  uint64_t overlap_warn_steps; /* steps with an overlap > 20 % of a radius */
+  uint64_t status_bits;        /* RP_STATUS_* seen since creation */
+  uint64_t neighbor_capacity;  /* list slots per particle */
+  uint64_t max_neighbors;      /* longest list at the last rebuild */
+  double kinetic_energy;       /* FP64, translational + rotational, at the last rp_get_stats */
+  double device_ms;            /* device time of the stepping calls so far */
+} rp_stats;
+
+#define RP_STATUS_OVERLAP 1u    /* overlap > 20 % of the smaller radius (src/simulation.rs:361-370) */
+#define RP_STATUS_NAN_FORCE 2u  /* a non-finite particle force */
+#define RP_STATUS_NLIST_GROW 4u /* a neighbour list outgrew its capacity (recovered) */
+
+/* --- lifecycle: Simulation.create (src/lib.rs:57, src/simulation.rs:62-91) */
+rp_sim* rp_create(double dt, const double min_xyz[3], const double max_xyz[3], size_t particle_capacity);
+void rp_destroy(rp_sim* sim);
+
+/* --- Simulation.add_particle (src/lib.rs:76-80, src/simulation.rs:93-96) */
+int rp_add_particle(rp_sim* sim, double x, double y, double z, double radius, double mass, int fixed);
+/* Bulk form of rp_add_particle: n particles, xyz holds 3n doubles; fixed may be NULL. */
+int rp_add_particles(rp_sim* sim, size_t n, const double* xyz, const double* radius, const double* mass,
+                     const uint8_t* fixed);
+
+/* --- Simulation.add_mesh (src/lib.rs:87-91, src/mesh.rs:125-143): binary or ASCII STL */
+int rp_add_mesh_stl(rp_sim* sim, const char* path);
+/* Triangles given directly: 9 floats per triangle (v0,v1,v2) and 3 per normal
+ * (NULL computes (v1-v0)x(v2-v0) normalised). */
+int rp_add_mesh_triangles(rp_sim* sim, size_t n_triangles, const float* vertices, const float* normals);
+
+/* --- Simulation.set_particle_material / set_wall_material (src/lib.rs:98-129) */
+int rp_set_particle_material(rp_sim* sim, double youngs_modulus, double poissons_ratio, double density,
+                             double friction_coefficient, double restitution_coefficient, double surface_energy);
+int rp_set_wall_material(rp_sim* sim, double youngs_modulus, double poissons_ratio, double density,
+                         double friction_coefficient, double restitution_coefficient, double surface_energy);
+
+/* --- Simulation.set_contact_models (src/lib.rs:160-180) */
+int rp_set_contact_models(rp_sim* sim, int normal_model, int tangential_model);
+/* The reference's case-insensitive name table (src/lib.rs:163-175); returns
+ * RP_E_INVALID_ARG for an unknown name. */
+int rp_parse_contact_models(const char* normal, const char* tangential, int* normal_model, int* tangential_model);
+
+/* --- Simulation.set_periodic_boundary (src/lib.rs:138) */
+int rp_set_periodic(rp_sim* sim, int x, int y, int z);
+
+/* --- Simulation.enable_gpu (src/lib.rs:146-148, src/simulation.rs:129-146):
+ * selects CUDA device `device` (-1 = current) and uploads the particles. */
+int rp_enable_gpu(rp_sim* sim, int device);
+
+/* --- Simulation.step / run (src/lib.rs:94, 182-195, src/simulation.rs:156-171) */
+int rp_step(rp_sim* sim, uint64_t n_steps);
+/* steps = ceil(duration / dt) evaluated in f32, as src/lib.rs:356 does. */
+int rp_run(rp_sim* sim, double duration);
+
+/* --- getters and setters (src/lib.rs:210-276); id out of range -> RP_E_INDEX */
+size_t rp_particle_count(rp_sim* sim);
+int rp_get_particle_position(rp_sim* sim, size_t id, double out_xyz[3]);
+int rp_get_particle_velocity(rp_sim* sim, size_t id, double out_xyz[3]);
+int rp_get_particle_angular_velocity(rp_sim* sim, size_t id, double out_xyz[3]);
+int rp_set_particle_velocity(rp_sim* sim, size_t id, double vx, double vy, double vz);
+int rp_set_particle_angular_velocity(rp_sim* sim, size_t id, double wx, double wy, double wz);
+
+/* --- Simulation.write_vtk (src/lib.rs:202-207, src/vtk.rs:5-44) */
+int rp_write_vtk(rp_sim* sim, const char* path);
+
+/* --- bulk state transfer (no reference counterpart; replaces the wgpu
+ * upload/readback of src/gpu.rs:92-98 and src/gpu.rs:168-213) */
+int rp_read_state(rp_sim* sim, rp_state* out);
+int rp_write_state(rp_sim* sim, const rp_state* in);
+
+/* --- options with the reference's hard-coded values as defaults */
+int rp_set_precision(rp_sim* sim, int precision);        /* RP_PREC_*; default FP64 */
+int rp_set_interaction_mode(rp_sim* sim, int mode);      /* RP_MODE_*; default PARITY */
+int rp_set_gravity(rp_sim* sim, double gx, double gy, double gz); /* default (0,-9.81,0), src/simulation.rs:267 */
+int rp_set_reference_cell_size(rp_sim* sim, double h);   /* default 1.0, src/simulation.rs:66 */
+int rp_set_skin(rp_sim* sim, double skin);               /* Verlet skin; <= 0 selects the default */
+int rp_set_threads(int n);                               /* set_num_threads (src/lib.rs:15-22) */
+
+/* --- metrics and errors */
+int rp_get_stats(rp_sim* sim, rp_stats* out);
+const char* rp_last_error(void);
+const char* rp_version(void);
+
+/* --- diagnostics for parity checks (no reference counterpart) */
+/* Record per-particle force/torque and contact multiplicities during steps. */
+int rp_set_debug(rp_sim* sim, int enable);
+/* Per-particle (f_total, torque_total) of the last step, before division by
+ * mass (src/simulation.rs:317-526), in id order; 3N doubles each. */
+int rp_debug_last_forces(rp_sim* sim, double* force, double* torque);
+/* Contact pairs of the last step seen from particle i: (i, j, visits) with
+ * visits the number of times the reference's loop would visit j
+ * (src/simulation.rs:322-357). Returns the pair count in *n; pass NULL arrays
+ * to query the count. */
+int rp_debug_contact_pairs(rp_sim* sim, int64_t* pi, int64_t* pj, int32_t* visits, size_t capacity, size_t* n);
+/* Runs the device cell-hash + radix-sort chain with the reference grid
+ * (src/grid.rs:12-46: cell size h, origin min, dims = ceil(size/h)+1) on the
+ * current positions. cell_of[i] = linear cell of particle i or -1 if outside
+ * the grid; order[] = particle ids grouped by cell, stable in id order
+ * (the flattened `cells` vectors); *n_order = number of inserted particles. */
+int rp_debug_reference_grid(rp_sim* sim, double h, int64_t* cell_of, int64_t* order, size_t* n_order,
+                            int32_t dims[3]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RP_H */

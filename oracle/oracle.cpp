@@ -324,6 +324,7 @@ struct Sim : Base {
 
   // last-step diagnostics
   std::vector<V3<T>> lastF, lastT;
+  std::vector<double> lastFS, lastTS;  // sums of |f_contact| and |r x f| per particle (summation-order scale)
   std::vector<uint64_t> pair_i, pair_j;  // pairs within cutoff, one entry per visit (i-side)
   bool record_pairs = false;
   std::mutex pair_mut;
@@ -482,7 +483,7 @@ struct Sim : Base {
   // One pair interaction seen from particle p (src/simulation.rs:327-461).
   // Returns false when outside the cutoff.
   inline bool pair_force(const Particle<T>& p, const Particle<T>& o, size_t i, size_t j, T es, T gs,
-                         V3<T>& ftot, V3<T>& ttot, bool& excessive, Hist* hp, bool& in_contact) {
+                         V3<T>& ftot, V3<T>& ttot, bool& excessive, Hist* hp, bool& in_contact, double& fs, double& ts) {
     V3<T> size = bmax - bmin;
     V3<T> d = p.x - o.x;
     if (periodic[0]) { if (d.x > size.x * T(0.5)) d.x = d.x - size.x; else if (d.x < -size.x * T(0.5)) d.x = d.x + size.x; }
@@ -547,7 +548,10 @@ struct Sim : Base {
     }
     V3<T> fc = fnv + ft;
     ftot += fc;
-    ttot += ra.cross(fc);
+    V3<T> tc = ra.cross(fc);
+    ttot += tc;
+    fs += (double)fc.length();
+    ts += (double)tc.length();
     return true;
   }
 
@@ -616,6 +620,8 @@ struct Sim : Base {
     T ew = effective_youngs(pm.E, pm.nu, wm.E, wm.nu);
     lastF.assign(n, V3<T>());
     lastT.assign(n, V3<T>());
+    lastFS.assign(n, 0.0);
+    lastTS.assign(n, 0.0);
     pair_i.clear(); pair_j.clear();
     int excessive_any = 0;
 #pragma omp parallel for schedule(dynamic, 64) reduction(| : excessive_any) if (par)
@@ -623,6 +629,7 @@ struct Sim : Base {
       size_t i = (size_t)il;
       const Particle<T>& p = ps[i];
       V3<T> ftot, ttot;
+      double fs = 0.0, ts = 0.0;
       bool excessive = false;
       std::vector<Hist> nh;
       std::vector<uint64_t> li, lj;
@@ -630,7 +637,7 @@ struct Sim : Base {
         for_candidates(p, [&](uint32_t j) {
           if (j == i) return;
           bool ic;
-          if (pair_force(p, ps[j], i, j, es, gs, ftot, ttot, excessive, nullptr, ic) && record_pairs) {
+          if (pair_force(p, ps[j], i, j, es, gs, ftot, ttot, excessive, nullptr, ic, fs, ts) && record_pairs) {
             li.push_back(i); lj.push_back(j);
           }
         });
@@ -642,7 +649,7 @@ struct Sim : Base {
           auto it = std::lower_bound(old.begin(), old.end(), h.tag, [](const Hist& a, uint64_t t) { return a.tag < t; });
           if (it != old.end() && it->tag == h.tag) h.xi = it->xi;
           bool ic;
-          if (pair_force(p, ps[j], i, j, es, gs, ftot, ttot, excessive, &h, ic)) {
+          if (pair_force(p, ps[j], i, j, es, gs, ftot, ttot, excessive, &h, ic, fs, ts)) {
             if (record_pairs) { li.push_back(i); lj.push_back(j); }
             if (ic) nh.push_back(h);
           }
@@ -669,10 +676,15 @@ struct Sim : Base {
         V3<T> ft = coulomb(fn, rv, nrm, pm.mu);
         V3<T> fc = fnv + ft;
         ftot += fc;
-        ttot += ra.cross(fc);
+        V3<T> tc = ra.cross(fc);
+        ttot += tc;
+        fs += (double)fc.length();
+        ts += (double)tc.length();
       }
       lastF[i] = ftot;
       lastT[i] = ttot;
+      lastFS[i] = fs;
+      lastTS[i] = ts;
       if (excessive) excessive_any = 1;
       if (mode == MODE_PHYSICAL) {
         std::sort(nh.begin(), nh.end(), [](const Hist& a, const Hist& b) { return a.tag < b.tag; });
@@ -872,6 +884,13 @@ void orc_last_forces(void* hv, double* F, double* Tq) {
       F[3 * i] = s->lastF[i].x; F[3 * i + 1] = s->lastF[i].y; F[3 * i + 2] = s->lastF[i].z;
       Tq[3 * i] = s->lastT[i].x; Tq[3 * i + 1] = s->lastT[i].y; Tq[3 * i + 2] = s->lastT[i].z;
     }
+    return 0;
+  });
+}
+// Per-particle sums of contribution magnitudes of the last step.
+void orc_last_force_scale(void* hv, double* FS, double* TS) {
+  dispatch((Handle*)hv, [&](auto* s) {
+    for (size_t i = 0; i < s->lastFS.size(); ++i) { FS[i] = s->lastFS[i]; TS[i] = s->lastTS[i]; }
     return 0;
   });
 }

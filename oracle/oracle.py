@@ -74,6 +74,7 @@ def lib():
             "orc_set_vec": (None, [vp, i, dp]),
             "orc_get_scalar": (None, [vp, i, dp]),
             "orc_last_forces": (None, [vp, dp, dp]),
+            "orc_last_force_scale": (None, [vp, dp, dp]),
             "orc_grid_dims": (None, [vp, ip]),
             "orc_grid_items": (l, [vp, lp, lp]),
             "orc_grid_now": (i, [vp]),
@@ -288,6 +289,15 @@ class OracleSimulation:
         if n:
             self._L.orc_last_forces(self._h, _dp(F), _dp(T))
         return F, T
+
+    def last_force_scale(self):
+        """Per-particle sums of |f_ij| and |r x f_ij| of the last step."""
+        n = self.get_particle_count()
+        FS = np.zeros(n)
+        TS = np.zeros(n)
+        if n:
+            self._L.orc_last_force_scale(self._h, _dp(FS), _dp(TS))
+        return FS, TS
 
     def grid(self, now=True):
         """Reference grid for the current positions: (dims, cell per particle, flattened order)."""

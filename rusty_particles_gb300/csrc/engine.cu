@@ -1,0 +1,877 @@
+// Host engine: particle store, device buffers and step sequencing.
+//
+// A step is launched as: first half (boundary, kick, drift) -> gated rebuild
+// chain (hash, radix sort, cell bounds, reorder, Verlet lists) -> forces +
+// second half -> end-of-step bookkeeping. Steps are issued in chunks with one
+// host synchronisation per chunk; a device control block reports completed
+// steps, rebuilds, removals and a halt when a neighbour list outgrew its
+// capacity (the engine then grows the lists and resumes the halted step).
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+
+#include "engine.h"
+
+namespace rp {
+
+void set_error(const char* fmt, ...);
+
+#define CK(x)                                                                 \
+  do {                                                                        \
+    cudaError_t e_ = (x);                                                     \
+    if (e_ != cudaSuccess) {                                                  \
+      set_error("%s failed: %s", #x, cudaGetErrorString(e_));                 \
+      return RP_E_CUDA;                                                       \
+    }                                                                         \
+  } while (0)
+
+#define TRY(x)               \
+  do {                       \
+    int r_ = (x);            \
+    if (r_ != RP_OK) return r_; \
+  } while (0)
+
+static const double kPiH = 3.14159265358979323846;
+
+// src/material.rs:33-37 (same operation order as the oracle)
+static double eff_youngs(double e1, double nu1, double e2, double nu2) {
+  double inv = (1.0 - nu1 * nu1) / e1 + (1.0 - nu2 * nu2) / e2;
+  return 1.0 / inv;
+}
+static double shear_mod(double e, double nu) { return e / (2.0 * (1.0 + nu)); }
+static double physical_shear(double e1, double nu1, double e2, double nu2) {
+  double g1 = shear_mod(e1, nu1), g2 = shear_mod(e2, nu2);
+  return 1.0 / ((2.0 - nu1) / g1 + (2.0 - nu2) / g2);
+}
+static int bits_for(uint64_t maxkey) {
+  int b = 1;
+  while (b < 32 && (1ull << b) <= maxkey) ++b;
+  return b;
+}
+template <typename T>
+static int dalloc(T** p, size_t count) {
+  if (*p) {
+    cudaFree(*p);
+    *p = nullptr;
+  }
+  if (count == 0) count = 1;
+  cudaError_t e = cudaMalloc((void**)p, sizeof(T) * count);
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    set_error("cudaMalloc of %zu bytes failed: %s", sizeof(T) * count, cudaGetErrorString(e));
+    return RP_E_NOMEM;
+  }
+  return RP_OK;
+}
+template <typename T>
+static void dfree(T*& p) {
+  if (p) cudaFree(p);
+  p = nullptr;
+}
+
+Engine::Engine(double dt_, const double mn[3], const double mx[3], size_t capacity) : dt(dt_) {
+  for (int k = 0; k < 3; ++k) {
+    bmin[k] = mn[k];
+    bmax[k] = mx[k];
+  }
+  hp_.reserve(capacity);
+}
+
+Engine::~Engine() { free_device(); }
+
+void Engine::free_device() {
+  if (!gpu_) return;
+  cudaSetDevice(device_);
+  for (int b = 0; b < 2; ++b) {
+    Bank& B = bank_[b];
+    dfree(B.xr); dfree(B.vm); dfree(B.wc); dfree(B.acc); dfree(B.tq);
+    dfree(B.xres); dfree(B.vres); dfree(B.wres); dfree(B.flags); dfree(B.tag); dfree(B.xref);
+    dfree(B.nbr); dfree(B.ncnt); dfree(B.hist);
+  }
+  dfree(rb_.ka); dfree(rb_.va); dfree(rb_.kb); dfree(rb_.vb); dfree(rb_.hist); dfree(rb_.part);
+  dfree(rb_.cstart); dfree(rb_.cend); dfree(kraw_);
+  dfree(dbgF_); dfree(dbgT_); dfree(dbgMult_); dfree(ke_);
+  dfree(tri_d_); dfree(tstart_d_); dfree(titems_d_);
+  dfree(ctrl_);
+  if (ctrl_h_) cudaFreeHost(ctrl_h_);
+  ctrl_h_ = nullptr;
+  if (ev0_) cudaEventDestroy(ev0_);
+  if (ev1_) cudaEventDestroy(ev1_);
+  if (stream_) cudaStreamDestroy(stream_);
+  stream_ = nullptr;
+  ev0_ = ev1_ = nullptr;
+  gpu_ = false;
+}
+
+int Engine::ensure_gpu() {
+  if (gpu_) {
+    CK(cudaSetDevice(device_));
+    return RP_OK;
+  }
+  int cnt = 0;
+  cudaError_t e = cudaGetDeviceCount(&cnt);
+  if (e != cudaSuccess || cnt == 0) {
+    set_error("no usable CUDA device: %s", e != cudaSuccess ? cudaGetErrorString(e) : "device count is 0");
+    return RP_E_CUDA;
+  }
+  if (device_ < 0) CK(cudaGetDevice(&device_));
+  if (device_ >= cnt) {
+    set_error("CUDA device %d does not exist (%d present)", device_, cnt);
+    return RP_E_CUDA;
+  }
+  CK(cudaSetDevice(device_));
+  CK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+  CK(cudaEventCreate(&ev0_));
+  CK(cudaEventCreate(&ev1_));
+  TRY(dalloc(&ctrl_, 1));
+  CK(cudaMallocHost((void**)&ctrl_h_, sizeof(Ctrl)));
+  TRY(dalloc(&ke_, 1));
+  gpu_ = true;
+  return RP_OK;
+}
+
+int Engine::enable_gpu(int device) {
+  if (gpu_ && device >= 0 && device != device_) {
+    if (!host_valid_) TRY(download());
+    free_device();
+    dev_valid_ = false;
+  }
+  if (!gpu_ && device >= 0) device_ = device;
+  TRY(ensure_gpu());
+  if (!dev_valid_) {
+    if (!host_valid_) TRY(download());
+    TRY(upload());
+  }
+  return RP_OK;
+}
+
+int Engine::add_particle(const double x[3], double r, double m, int fixed) {
+  if (!host_valid_) TRY(download());
+  HostParticle p;
+  std::memset(&p, 0, sizeof(p));
+  for (int k = 0; k < 3; ++k) p.x[k] = x[k];
+  p.r = r;
+  p.m = m;
+  p.fixed = fixed ? 1 : 0;
+  p.tag = next_tag_++;
+  hp_.push_back(p);
+  dev_valid_ = false;
+  return RP_OK;
+}
+
+int Engine::add_triangles(size_t n, const float* v, const float* nrm) {
+  for (size_t t = 0; t < n; ++t) {
+    const float* q = v + 9 * t;
+    for (int k = 0; k < 9; ++k) tri_v_.push_back(q[k]);
+    if (nrm) {
+      for (int k = 0; k < 3; ++k) tri_n_.push_back(nrm[3 * t + k]);
+    } else {
+      double e0[3] = {(double)q[3] - q[0], (double)q[4] - q[1], (double)q[5] - q[2]};
+      double e1[3] = {(double)q[6] - q[0], (double)q[7] - q[1], (double)q[8] - q[2]};
+      double c[3] = {e0[1] * e1[2] - e0[2] * e1[1], e0[2] * e1[0] - e0[0] * e1[2], e0[0] * e1[1] - e0[1] * e1[0]};
+      double l = std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+      for (int k = 0; k < 3; ++k) tri_n_.push_back(l > 0 ? (float)(c[k] / l) : 0.f);
+    }
+  }
+  dev_valid_ = false;
+  return RP_OK;
+}
+
+size_t Engine::count() {
+  if (!host_valid_) {
+    if (download() != RP_OK) return 0;
+  }
+  return hp_.size();
+}
+
+// ------------------------------------------------------------- allocation
+int Engine::alloc_slots(size_t n) {
+  size_t na = std::max<size_t>(n, 1);
+  na = (na + 1023) & ~size_t(1023);
+  for (int b = 0; b < 2; ++b) {
+    Bank& B = bank_[b];
+    TRY(dalloc(&B.xr, na)); TRY(dalloc(&B.vm, na)); TRY(dalloc(&B.wc, na)); TRY(dalloc(&B.acc, na));
+    TRY(dalloc(&B.tq, na)); TRY(dalloc(&B.xres, na)); TRY(dalloc(&B.vres, na)); TRY(dalloc(&B.wres, na));
+    TRY(dalloc(&B.flags, na)); TRY(dalloc(&B.tag, na)); TRY(dalloc(&B.xref, na)); TRY(dalloc(&B.ncnt, na));
+  }
+  TRY(dalloc(&rb_.ka, na)); TRY(dalloc(&rb_.va, na)); TRY(dalloc(&rb_.kb, na)); TRY(dalloc(&rb_.vb, na));
+  TRY(dalloc(&kraw_, na));
+  uint32_t hn = radix_hist_needed((uint32_t)na);
+  TRY(dalloc(&rb_.hist, hn));
+  TRY(dalloc(&rb_.part, scan_parts_needed(std::max<uint32_t>(hn, (uint32_t)na)) + 16));
+  TRY(dalloc(&dbgF_, 3 * na)); TRY(dalloc(&dbgT_, 3 * na));
+  n_alloc_ = na;
+  // lists must be re-allocated for the new slot count
+  for (int b = 0; b < 2; ++b) {
+    dfree(bank_[b].nbr);
+    dfree(bank_[b].hist);
+  }
+  dfree(dbgMult_);
+  return RP_OK;
+}
+
+int Engine::alloc_lists(int cap, bool keep_current) {
+  const bool need_hist = (mode == RP_MODE_PHYSICAL && tmodel != RP_TANGENTIAL_COULOMB);
+  const size_t na = n_alloc_;
+  const int cur = keep_current ? last_.bank : 0;
+  uint32_t* old_nbr = keep_current ? bank_[cur].nbr : nullptr;
+  double* old_hist = keep_current ? bank_[cur].hist : nullptr;
+  const int old_cap = cap_;
+  for (int b = 0; b < 2; ++b) {
+    uint32_t* nb = nullptr;
+    TRY(dalloc(&nb, na * (size_t)cap));
+    double* nh = nullptr;
+    if (need_hist) {
+      TRY(dalloc(&nh, 3 * na * (size_t)cap));
+      CK(cudaMemsetAsync(nh, 0, sizeof(double) * 3 * na * (size_t)cap, stream_));
+    }
+    if (keep_current && b == cur && old_nbr && n_ > 0) {
+      CK(cudaMemcpy2DAsync(nb, sizeof(uint32_t) * cap, old_nbr, sizeof(uint32_t) * old_cap,
+                           sizeof(uint32_t) * old_cap, n_, cudaMemcpyDeviceToDevice, stream_));
+      if (need_hist && old_hist) {
+        for (int p = 0; p < 3; ++p)
+          CK(cudaMemcpy2DAsync(nh + (size_t)p * n_ * cap, sizeof(double) * cap, old_hist + (size_t)p * n_ * old_cap,
+                               sizeof(double) * old_cap, sizeof(double) * old_cap, n_, cudaMemcpyDeviceToDevice,
+                               stream_));
+      }
+    }
+    CK(cudaStreamSynchronize(stream_));
+    dfree(bank_[b].nbr);
+    dfree(bank_[b].hist);
+    bank_[b].nbr = nb;
+    bank_[b].hist = nh;
+  }
+  if (debug) {
+    TRY(dalloc(&dbgMult_, na * (size_t)cap));
+    CK(cudaMemset(dbgMult_, 0, na * (size_t)cap));
+  } else {
+    dfree(dbgMult_);
+  }
+  cap_ = cap;
+  return RP_OK;
+}
+
+// ------------------------------------------------------------ parameters
+int Engine::build_params() {
+  StepParams& P = P_;
+  P.n = n_;
+  P.cap = cap_;
+  P.nmodel = nmodel;
+  P.tmodel = tmodel;
+  P.mode = mode;
+  P.prec = prec;
+  P.debug = debug;
+  P.dt = dt;
+  for (int k = 0; k < 3; ++k) {
+    P.periodic[k] = periodic[k] ? 1 : 0;
+    P.bmin[k] = bmin[k];
+    P.bmax[k] = bmax[k];
+    P.bsize[k] = bmax[k] - bmin[k];
+    P.gravity[k] = gravity[k];
+  }
+  P.pm = pm;
+  P.wm = wm;
+  P.es_pp = eff_youngs(pm.E, pm.nu, pm.E, pm.nu);
+  P.es_pw = eff_youngs(pm.E, pm.nu, wm.E, wm.nu);
+  P.gs_pp = mode == RP_MODE_PARITY ? 0.0 : physical_shear(pm.E, pm.nu, pm.E, pm.nu);
+  P.gamma_pp = (pm.gamma + pm.gamma) * 0.5;
+  P.gamma_pw = (pm.gamma + wm.gamma) * 0.5;
+  {
+    double ln_e = std::log(pm.e);
+    double beta = ln_e / std::sqrt(ln_e * ln_e + kPiH * kPiH);
+    P.beta_abs = std::fabs(beta);
+  }
+  // reference grid: dims = ceil(size / h) + 1 (src/grid.rs:13)
+  P.href = href;
+  for (int k = 0; k < 3; ++k) {
+    double q = std::ceil(P.bsize[k] / href);
+    if (!(q >= 0.0) || q > (double)((1 << 20) - 4)) {
+      if (mode == RP_MODE_PARITY) {
+        set_error("reference grid too large on axis %d (%g cells); parity mode needs < 2^20 cells per axis", k, q);
+        return RP_E_INVALID_ARG;
+      }
+      q = 1.0;
+    }
+    P.rdims[k] = (int)q + 1;
+  }
+  // fine grid: cell >= largest list radius
+  double rmax = 0.0;
+  for (const HostParticle& p : hp_) rmax = std::max(rmax, p.r);
+  const double adh = (nmodel == RP_NORMAL_JKR || nmodel == RP_NORMAL_SJKR) ? 1.5 : 1.0;
+  double skin = skin_user > 0.0 ? skin_user : 0.1 * 2.0 * rmax;
+  if (!(skin > 0.0)) skin = 1e-6;
+  P.skin = skin;
+  P.list_scale = 1.0f + 1e-5f;
+  double h = 2.0 * rmax * adh + skin;
+  if (!(h > 0.0)) h = 1.0;
+  const uint64_t max_cells = std::max<uint64_t>(4ull * (uint64_t)n_ + (1ull << 16), 1ull << 20);
+  for (int iter = 0; iter < 64; ++iter) {
+    uint64_t tot = 1;
+    for (int k = 0; k < 3; ++k) {
+      double L = P.bsize[k];
+      double d = periodic[k] ? std::floor(L / h) : std::ceil(L / h);
+      if (!(d >= 1.0)) d = 1.0;
+      if (d > 1e6) d = 1e6;
+      P.fdims[k] = (int)d;
+      P.fcell[k] = periodic[k] ? L / d : h;
+      if (!(P.fcell[k] >= h)) P.fcell[k] = h;
+      P.fmin[k] = bmin[k];
+      tot *= (uint64_t)P.fdims[k];
+    }
+    if (tot <= max_cells) break;
+    h *= 1.25;
+  }
+  P.fncells = (uint32_t)((uint64_t)P.fdims[0] * P.fdims[1] * P.fdims[2]);
+  rb_.key_bits = bits_for(P.fncells);
+  rb_.carry_history = (mode == RP_MODE_PHYSICAL && tmodel != RP_TANGENTIAL_COULOMB) ? 1 : 0;
+  if (P.fncells > fcells_alloc_) {
+    TRY(dalloc(&rb_.cstart, P.fncells));
+    TRY(dalloc(&rb_.cend, P.fncells));
+    fcells_alloc_ = P.fncells;
+  }
+  TRY(build_triangle_grid(rmax));
+  P.dbgF = dbgF_;
+  P.dbgT = dbgT_;
+  P.dbgMult = dbgMult_;
+  P.ctrl = ctrl_;
+  P.bank[0] = bank_[0];
+  P.bank[1] = bank_[1];
+  return RP_OK;
+}
+
+// Uniform grid over the triangles: each triangle is listed in every cell its
+// bounding box, grown by the largest particle radius, overlaps; a particle
+// then tests only the triangles of the cell holding its centre. Lists keep
+// triangle (mesh) order, so contributions sum in the reference's order
+// (src/simulation.rs:465-466).
+int Engine::build_triangle_grid(double rmax) {
+  const size_t T = tri_v_.size() / 9;
+  P_.ntri = (int)T;
+  if (T == 0) {
+    P_.tri = nullptr;
+    P_.tstart = nullptr;
+    P_.titems = nullptr;
+    return RP_OK;
+  }
+  std::vector<TriRec> recs(T);
+  double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+  std::vector<double> blo(3 * T), bhi(3 * T);
+  const double grow = rmax * (1.0 + 1e-9) + 1e-12;
+  for (size_t t = 0; t < T; ++t) {
+    const float* q = &tri_v_[9 * t];
+    TriRec& r = recs[t];
+    double v0[3] = {q[0], q[1], q[2]}, v1[3] = {q[3], q[4], q[5]}, v2[3] = {q[6], q[7], q[8]};
+    for (int k = 0; k < 3; ++k) {
+      r.v0[k] = v0[k];
+      r.e0[k] = v1[k] - v0[k];
+      r.e1[k] = v2[k] - v0[k];
+      r.n[k] = tri_n_[3 * t + k];
+    }
+    r.a = r.e0[0] * r.e0[0] + r.e0[1] * r.e0[1] + r.e0[2] * r.e0[2];
+    r.b = r.e0[0] * r.e1[0] + r.e0[1] * r.e1[1] + r.e0[2] * r.e1[2];
+    r.c = r.e1[0] * r.e1[0] + r.e1[1] * r.e1[1] + r.e1[2] * r.e1[2];
+    r.det = r.a * r.c - r.b * r.b;
+    r.denom = r.a - 2.0 * r.b + r.c;
+    r.pad = 0.0;
+    for (int k = 0; k < 3; ++k) {
+      double mn = std::min(v0[k], std::min(v1[k], v2[k])) - grow;
+      double mx = std::max(v0[k], std::max(v1[k], v2[k])) + grow;
+      blo[3 * t + k] = mn;
+      bhi[3 * t + k] = mx;
+      lo[k] = std::min(lo[k], mn);
+      hi[k] = std::max(hi[k], mx);
+    }
+  }
+  double ext = std::max(hi[0] - lo[0], std::max(hi[1] - lo[1], hi[2] - lo[2]));
+  double cell = std::max(2.0 * rmax, ext / 1024.0);
+  if (!(cell > 0.0)) cell = 1.0;
+  std::vector<uint32_t> counts;
+  int dims[3];
+  uint64_t entries = 0;
+  for (int iter = 0; iter < 80; ++iter) {
+    uint64_t tot = 1;
+    for (int k = 0; k < 3; ++k) {
+      dims[k] = std::max(1, (int)std::ceil((hi[k] - lo[k]) / cell));
+      tot *= (uint64_t)dims[k];
+    }
+    if (tot > (1ull << 24)) {
+      cell *= 1.5;
+      continue;
+    }
+    entries = 0;
+    for (size_t t = 0; t < T; ++t) {
+      uint64_t c = 1;
+      for (int k = 0; k < 3; ++k) {
+        int a = std::max(0, (int)std::floor((blo[3 * t + k] - lo[k]) / cell));
+        int b = std::min(dims[k] - 1, (int)std::floor((bhi[3 * t + k] - lo[k]) / cell));
+        c *= (uint64_t)(b - a + 1);
+      }
+      entries += c;
+    }
+    if (entries <= 64ull * T + (1ull << 22)) break;
+    cell *= 1.5;
+  }
+  const size_t nc = (size_t)dims[0] * dims[1] * dims[2];
+  std::vector<uint32_t> start(nc + 1, 0);
+  auto for_cells = [&](size_t t, auto&& f) {
+    int a[3], b[3];
+    for (int k = 0; k < 3; ++k) {
+      a[k] = std::max(0, (int)std::floor((blo[3 * t + k] - lo[k]) / cell));
+      b[k] = std::min(dims[k] - 1, (int)std::floor((bhi[3 * t + k] - lo[k]) / cell));
+    }
+    for (int z = a[2]; z <= b[2]; ++z)
+      for (int y = a[1]; y <= b[1]; ++y)
+        for (int x = a[0]; x <= b[0]; ++x) f((size_t)x + (size_t)dims[0] * ((size_t)y + (size_t)dims[1] * z));
+  };
+  for (size_t t = 0; t < T; ++t) for_cells(t, [&](size_t c) { start[c + 1]++; });
+  for (size_t c = 0; c < nc; ++c) start[c + 1] += start[c];
+  std::vector<uint32_t> items(start[nc]);
+  std::vector<uint32_t> fill(start.begin(), start.end() - 1);
+  for (size_t t = 0; t < T; ++t) for_cells(t, [&](size_t c) { items[fill[c]++] = (uint32_t)t; });
+  TRY(dalloc(&tri_d_, T));
+  TRY(dalloc(&tstart_d_, nc + 1));
+  TRY(dalloc(&titems_d_, std::max<size_t>(items.size(), 1)));
+  CK(cudaMemcpy(tri_d_, recs.data(), sizeof(TriRec) * T, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(tstart_d_, start.data(), sizeof(uint32_t) * (nc + 1), cudaMemcpyHostToDevice));
+  if (!items.empty()) CK(cudaMemcpy(titems_d_, items.data(), sizeof(uint32_t) * items.size(), cudaMemcpyHostToDevice));
+  P_.tri = tri_d_;
+  P_.tstart = tstart_d_;
+  P_.titems = titems_d_;
+  for (int k = 0; k < 3; ++k) {
+    P_.tmin[k] = lo[k];
+    P_.tdims[k] = dims[k];
+  }
+  P_.tcell = cell;
+  return RP_OK;
+}
+
+// --------------------------------------------------------- upload/download
+int Engine::upload() {
+  TRY(ensure_gpu());
+  for (const HostParticle& p : hp_) {
+    if (!(p.r > 0.0) || !(p.m > 0.0)) {
+      set_error("particle radius and mass must be positive");
+      return RP_E_INVALID_ARG;
+    }
+  }
+  const size_t n = hp_.size();
+  if (n > (size_t)0x7FFFFFF0) {
+    set_error("too many particles");
+    return RP_E_INVALID_ARG;
+  }
+  n_ = (int)n;
+  if (n > n_alloc_ || n_alloc_ == 0) TRY(alloc_slots(n));
+  if (cap_ == 0) cap_ = 32;
+  const bool need_hist = (mode == RP_MODE_PHYSICAL && tmodel != RP_TANGENTIAL_COULOMB);
+  if (!bank_[0].nbr || (need_hist && !bank_[0].hist) || (debug && !dbgMult_)) TRY(alloc_lists(cap_, false));
+  // pack
+  const size_t na = std::max<size_t>(n, 1);
+  std::vector<D4> a8[8];
+  for (auto& v : a8) v.resize(na);
+  std::vector<uint32_t> flags(na, 0), tags(na, 0);
+  for (size_t i = 0; i < n; ++i) {
+    const HostParticle& p = hp_[i];
+    a8[0][i] = D4{p.x[0], p.x[1], p.x[2], p.r};
+    a8[1][i] = D4{p.v[0], p.v[1], p.v[2], p.m};
+    a8[2][i] = D4{p.w[0], p.w[1], p.w[2], 0.0};
+    a8[3][i] = D4{p.a[0], p.a[1], p.a[2], 0.0};
+    a8[4][i] = D4{p.tau[0], p.tau[1], p.tau[2], 0.0};
+    a8[5][i] = D4{p.xres[0], p.xres[1], p.xres[2], 0.0};
+    a8[6][i] = D4{p.vres[0], p.vres[1], p.vres[2], 0.0};
+    a8[7][i] = D4{p.wres[0], p.wres[1], p.wres[2], 0.0};
+    flags[i] = p.fixed ? PF_FIXED : 0u;
+    tags[i] = p.tag;
+  }
+  Bank& B = bank_[0];
+  D4* dst[8] = {B.xr, B.vm, B.wc, B.acc, B.tq, B.xres, B.vres, B.wres};
+  if (n > 0) {
+    for (int q = 0; q < 8; ++q) CK(cudaMemcpy(dst[q], a8[q].data(), sizeof(D4) * n, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(B.flags, flags.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(B.tag, tags.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice));
+    std::vector<float4> xref(n, make_float4(NAN, NAN, NAN, 0.f));
+    CK(cudaMemcpy(B.xref, xref.data(), sizeof(float4) * n, cudaMemcpyHostToDevice));
+  }
+  for (int b = 0; b < 2; ++b) CK(cudaMemset(bank_[b].ncnt, 0, sizeof(uint32_t) * n_alloc_));
+  if (need_hist)
+    for (int b = 0; b < 2; ++b) CK(cudaMemset(bank_[b].hist, 0, sizeof(double) * 3 * n_alloc_ * (size_t)cap_));
+  TRY(build_params());
+  Ctrl c;
+  std::memset(&c, 0, sizeof(c));
+  c.bank = 0;
+  c.rebuild = 1;
+  CK(cudaMemcpy(ctrl_, &c, sizeof(Ctrl), cudaMemcpyHostToDevice));
+  last_ = c;
+  dev_valid_ = true;
+  return RP_OK;
+}
+
+int Engine::sync_ctrl() {
+  CK(cudaMemcpyAsync(ctrl_h_, ctrl_, sizeof(Ctrl), cudaMemcpyDeviceToHost, stream_));
+  CK(cudaStreamSynchronize(stream_));
+  return RP_OK;
+}
+
+int Engine::download() {
+  if (!gpu_ || !dev_valid_ || host_valid_) {
+    host_valid_ = true;
+    return RP_OK;
+  }
+  CK(cudaSetDevice(device_));
+  TRY(sync_ctrl());
+  const Bank& B = bank_[ctrl_h_->bank];
+  const size_t n = (size_t)n_;
+  std::vector<D4> a8[8];
+  const D4* src[8] = {B.xr, B.vm, B.wc, B.acc, B.tq, B.xres, B.vres, B.wres};
+  std::vector<uint32_t> flags(n), tags(n);
+  if (n > 0) {
+    for (int q = 0; q < 8; ++q) {
+      a8[q].resize(n);
+      CK(cudaMemcpy(a8[q].data(), src[q], sizeof(D4) * n, cudaMemcpyDeviceToHost));
+    }
+    CK(cudaMemcpy(flags.data(), B.flags, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(tags.data(), B.tag, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost));
+  }
+  std::vector<std::pair<uint32_t, size_t>> order;
+  order.reserve(n);
+  bool dead = false;
+  for (size_t k = 0; k < n; ++k) {
+    if (flags[k] & PF_DEAD) {
+      dead = true;
+      continue;
+    }
+    order.emplace_back(tags[k], k);
+  }
+  std::sort(order.begin(), order.end());
+  hp_.resize(order.size());
+  for (size_t i = 0; i < order.size(); ++i) {
+    size_t k = order[i].second;
+    HostParticle& p = hp_[i];
+    const D4* q[8];
+    for (int a = 0; a < 8; ++a) q[a] = &a8[a][k];
+    double* d[8] = {p.x, p.v, p.w, p.a, p.tau, p.xres, p.vres, p.wres};
+    for (int a = 0; a < 8; ++a) {
+      d[a][0] = q[a]->x;
+      d[a][1] = q[a]->y;
+      d[a][2] = q[a]->z;
+    }
+    p.r = a8[0][k].w;
+    p.m = a8[1][k].w;
+    p.fixed = (flags[k] & PF_FIXED) ? 1 : 0;
+    p.tag = tags[k];
+  }
+  host_valid_ = true;
+  if (dead) dev_valid_ = false;  // the next step re-uploads the compacted set
+  return RP_OK;
+}
+
+// ------------------------------------------------------------------ steps
+int Engine::finish_step_accounting() {
+  const Ctrl& c = *ctrl_h_;
+  tot_.steps += c.steps_done - last_.steps_done;
+  tot_.rebuilds += c.rebuilds - last_.rebuilds;
+  tot_.overlap_steps += c.overlap_steps - last_.overlap_steps;
+  tot_.removed += c.removed - last_.removed;
+  tot_.status |= c.status;
+  tot_.max_count = c.max_count;
+  last_ = c;
+  return RP_OK;
+}
+
+int Engine::launch_steps(uint64_t n, bool) {
+  const uint64_t CHUNK = 512;
+  uint64_t remaining = n;
+  while (remaining > 0) {
+    const uint64_t chunk = std::min(remaining, CHUNK);
+    const uint64_t before = last_.steps_done;
+    CK(cudaEventRecord(ev0_, stream_));
+    for (uint64_t s = 0; s < chunk; ++s) {
+      launch_first_half(P_, stream_);
+      launch_rebuild(P_, rb_, stream_);
+      launch_force(P_, stream_);
+      launch_end_step(P_, stream_);
+    }
+    CK(cudaEventRecord(ev1_, stream_));
+    CK(cudaGetLastError());
+    TRY(sync_ctrl());
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ev0_, ev1_);
+    ms_total_ += ms;
+    while (ctrl_h_->halt) {
+      // A list outgrew its capacity during the rebuild of the step after
+      // `steps_done`: grow the lists (keeping the current bank's rows for the
+      // history carry-over) and finish that step.
+      int newcap = std::max<int>(cap_ + 8, (int)(ctrl_h_->max_count * 5 / 4 + 8));
+      TRY(alloc_lists(newcap, true));
+      P_.cap = cap_;
+      P_.bank[0] = bank_[0];
+      P_.bank[1] = bank_[1];
+      P_.dbgMult = dbgMult_;
+      tot_.status |= ST_NLIST_GROW;
+      int zero = 0;
+      unsigned zu = 0;
+      CK(cudaMemcpyAsync(&ctrl_->halt, &zero, sizeof(int), cudaMemcpyHostToDevice, stream_));
+      CK(cudaMemcpyAsync(&ctrl_->max_count, &zu, sizeof(unsigned), cudaMemcpyHostToDevice, stream_));
+      CK(cudaStreamSynchronize(stream_));
+      launch_rebuild(P_, rb_, stream_);
+      launch_force(P_, stream_);
+      launch_end_step(P_, stream_);
+      CK(cudaGetLastError());
+      TRY(sync_ctrl());
+    }
+    TRY(finish_step_accounting());
+    const uint64_t done = last_.steps_done - before;
+    if (done == 0) {
+      set_error("device made no progress in a chunk of %llu steps", (unsigned long long)chunk);
+      return RP_E_DEVICE_FLAG;
+    }
+    remaining -= std::min(done, remaining);
+  }
+  return RP_OK;
+}
+
+int Engine::step(uint64_t n) {
+  TRY(ensure_gpu());
+  if (!dev_valid_) {
+    if (!host_valid_) TRY(download());
+    TRY(upload());
+  }
+  if (n == 0) return RP_OK;
+  if (n_ == 0) {
+    tot_.steps += n;
+    return RP_OK;
+  }
+  host_valid_ = false;
+  int r = launch_steps(n, false);
+  if (r != RP_OK) return r;
+  // many removals: compact through the host before the next step
+  if (last_.removed > 0 && last_.removed * 8 > (uint64_t)n_) {
+    TRY(download());
+  }
+  return RP_OK;
+}
+
+// ---------------------------------------------------------- state access
+int Engine::get_vec(size_t id, int which, double out[3]) {
+  if (!host_valid_) TRY(download());
+  if (id >= hp_.size()) {
+    set_error("Particle index out of bounds");
+    return RP_E_INDEX;
+  }
+  const HostParticle& p = hp_[id];
+  const double* s = which == 0 ? p.x : which == 1 ? p.v : p.w;
+  for (int k = 0; k < 3; ++k) out[k] = s[k];
+  return RP_OK;
+}
+
+int Engine::set_vec(size_t id, int which, const double in[3]) {
+  if (!host_valid_) TRY(download());
+  if (id >= hp_.size()) {
+    set_error("Particle index out of bounds");
+    return RP_E_INDEX;
+  }
+  HostParticle& p = hp_[id];
+  double* d = which == 1 ? p.v : p.w;
+  for (int k = 0; k < 3; ++k) d[k] = in[k];
+  dev_valid_ = false;
+  return RP_OK;
+}
+
+int Engine::read_state(rp_state* st) {
+  if (!host_valid_) TRY(download());
+  const size_t n = hp_.size();
+  st->n_particles = n;
+  double* vec[8] = {st->position, st->velocity, st->angular_velocity, st->acceleration,
+                    st->torque, st->position_residual, st->velocity_residual, st->angular_velocity_residual};
+  for (size_t i = 0; i < n; ++i) {
+    const HostParticle& p = hp_[i];
+    const double* s[8] = {p.x, p.v, p.w, p.a, p.tau, p.xres, p.vres, p.wres};
+    for (int a = 0; a < 8; ++a)
+      if (vec[a])
+        for (int k = 0; k < 3; ++k) vec[a][3 * i + k] = s[a][k];
+    if (st->radius) st->radius[i] = p.r;
+    if (st->mass) st->mass[i] = p.m;
+    if (st->fixed) st->fixed[i] = p.fixed;
+  }
+  return RP_OK;
+}
+
+int Engine::write_state(const rp_state* st) {
+  if (!host_valid_) TRY(download());
+  const size_t n = hp_.size();
+  const double* vec[8] = {st->position, st->velocity, st->angular_velocity, st->acceleration,
+                          st->torque, st->position_residual, st->velocity_residual, st->angular_velocity_residual};
+  for (size_t i = 0; i < n; ++i) {
+    HostParticle& p = hp_[i];
+    double* d[8] = {p.x, p.v, p.w, p.a, p.tau, p.xres, p.vres, p.wres};
+    for (int a = 0; a < 8; ++a)
+      if (vec[a])
+        for (int k = 0; k < 3; ++k) d[a][k] = vec[a][3 * i + k];
+    if (st->radius) p.r = st->radius[i];
+    if (st->mass) p.m = st->mass[i];
+    if (st->fixed) p.fixed = st->fixed[i] ? 1 : 0;
+  }
+  dev_valid_ = false;
+  return RP_OK;
+}
+
+int Engine::stats(rp_stats* s) {
+  std::memset(s, 0, sizeof(*s));
+  s->steps = tot_.steps;
+  s->removed = tot_.removed;
+  s->neighbor_rebuilds = tot_.rebuilds;
+  s->overlap_warn_steps = tot_.overlap_steps;
+  s->status_bits = tot_.status;
+  s->neighbor_capacity = (uint64_t)cap_;
+  s->max_neighbors = tot_.max_count;
+  s->device_ms = ms_total_;
+  if (gpu_ && dev_valid_ && n_ > 0) {
+    CK(cudaSetDevice(device_));
+    launch_kinetic_energy(P_, ke_, stream_);
+    double ke = 0.0;
+    CK(cudaMemcpyAsync(&ke, ke_, sizeof(double), cudaMemcpyDeviceToHost, stream_));
+    CK(cudaStreamSynchronize(stream_));
+    s->kinetic_energy = ke;
+    TRY(sync_ctrl());
+    s->particles = (uint64_t)n_ - (ctrl_h_->removed);
+  } else {
+    double ke = 0.0;
+    for (const HostParticle& p : hp_) {
+      double I = 0.4 * p.m * p.r * p.r;
+      ke += 0.5 * p.m * (p.v[0] * p.v[0] + p.v[1] * p.v[1] + p.v[2] * p.v[2]) +
+            0.5 * I * (p.w[0] * p.w[0] + p.w[1] * p.w[1] + p.w[2] * p.w[2]);
+    }
+    s->kinetic_energy = ke;
+    s->particles = hp_.size();
+  }
+  return RP_OK;
+}
+
+// ------------------------------------------------------------ diagnostics
+int Engine::debug_forces(double* F, double* T) {
+  if (!gpu_ || !debug) {
+    set_error("debug recording is off (call rp_set_debug before stepping)");
+    return RP_E_INVALID_ARG;
+  }
+  TRY(sync_ctrl());
+  const Bank& B = bank_[ctrl_h_->bank];
+  const size_t n = (size_t)n_;
+  std::vector<uint32_t> flags(n), tags(n);
+  std::vector<double> f(3 * n), t(3 * n);
+  if (n) {
+    CK(cudaMemcpy(flags.data(), B.flags, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(tags.data(), B.tag, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(f.data(), dbgF_, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(t.data(), dbgT_, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost));
+  }
+  std::vector<std::pair<uint32_t, size_t>> order;
+  for (size_t k = 0; k < n; ++k)
+    if (!(flags[k] & PF_DEAD)) order.emplace_back(tags[k], k);
+  std::sort(order.begin(), order.end());
+  for (size_t i = 0; i < order.size(); ++i) {
+    size_t k = order[i].second;
+    for (int a = 0; a < 3; ++a) {
+      F[3 * i + a] = f[3 * k + a];
+      T[3 * i + a] = t[3 * k + a];
+    }
+  }
+  return RP_OK;
+}
+
+int Engine::debug_pairs(int64_t* pi, int64_t* pj, int32_t* visits, size_t capacity, size_t* nout) {
+  if (!gpu_ || !debug || !dbgMult_) {
+    set_error("debug recording is off (call rp_set_debug before stepping)");
+    return RP_E_INVALID_ARG;
+  }
+  TRY(sync_ctrl());
+  const Bank& B = bank_[ctrl_h_->bank];
+  const size_t n = (size_t)n_;
+  std::vector<uint32_t> flags(n), tags(n), cnt(n), nbr(n * (size_t)cap_);
+  std::vector<uint8_t> mult(n * (size_t)cap_);
+  if (n) {
+    CK(cudaMemcpy(flags.data(), B.flags, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(tags.data(), B.tag, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(cnt.data(), B.ncnt, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(nbr.data(), B.nbr, sizeof(uint32_t) * n * cap_, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(mult.data(), dbgMult_, n * (size_t)cap_, cudaMemcpyDeviceToHost));
+  }
+  std::vector<std::pair<uint32_t, size_t>> order;
+  for (size_t k = 0; k < n; ++k)
+    if (!(flags[k] & PF_DEAD)) order.emplace_back(tags[k], k);
+  std::sort(order.begin(), order.end());
+  std::vector<int64_t> id_of(n, -1);
+  for (size_t i = 0; i < order.size(); ++i) id_of[order[i].second] = (int64_t)i;
+  size_t c = 0;
+  for (size_t k = 0; k < n; ++k) {
+    if (id_of[k] < 0) continue;
+    for (uint32_t m = 0; m < cnt[k]; ++m) {
+      uint8_t v = mult[k * cap_ + m];
+      if (!v) continue;
+      if (pi && c < capacity) {
+        pi[c] = id_of[k];
+        pj[c] = id_of[nbr[k * cap_ + m]];
+        visits[c] = v;
+      }
+      ++c;
+    }
+  }
+  *nout = c;
+  return RP_OK;
+}
+
+int Engine::debug_reference_grid(double h, int64_t* cell_of, int64_t* order, size_t* n_order, int32_t dims[3]) {
+  TRY(ensure_gpu());
+  if (!host_valid_) TRY(download());
+  const size_t n = hp_.size();
+  StepParams P = P_;
+  P.href = h;
+  uint64_t ncells = 1;
+  for (int k = 0; k < 3; ++k) {
+    P.bmin[k] = bmin[k];
+    double q = std::ceil((bmax[k] - bmin[k]) / h);
+    if (!(q >= 0.0) || q > 1e7) {
+      set_error("reference grid too large");
+      return RP_E_INVALID_ARG;
+    }
+    P.rdims[k] = (int)q + 1;
+    dims[k] = P.rdims[k];
+    ncells *= (uint64_t)P.rdims[k];
+  }
+  if (ncells >= 0xFFFFFFF0ull) {
+    set_error("reference grid too large");
+    return RP_E_INVALID_ARG;
+  }
+  if (n == 0) {
+    *n_order = 0;
+    return RP_OK;
+  }
+  if (n > n_alloc_) {
+    TRY(alloc_slots(n));
+    dev_valid_ = false;  // slot buffers were re-allocated; the next step re-uploads
+  }
+  std::vector<D4> xr(n);
+  for (size_t i = 0; i < n; ++i) xr[i] = D4{hp_[i].x[0], hp_[i].x[1], hp_[i].x[2], hp_[i].r};
+  D4* xr_d = nullptr;
+  TRY(dalloc(&xr_d, n));
+  CK(cudaMemcpy(xr_d, xr.data(), sizeof(D4) * n, cudaMemcpyHostToDevice));
+  int which = launch_reference_grid(P, xr_d, (int)n, (uint32_t)ncells, bits_for(ncells), kraw_, rb_.ka, rb_.va,
+                                    rb_.kb, rb_.vb, rb_.hist, rb_.part, stream_);
+  CK(cudaGetLastError());
+  std::vector<uint32_t> raw(n), sk(n), sv(n);
+  CK(cudaMemcpyAsync(raw.data(), kraw_, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, stream_));
+  CK(cudaMemcpyAsync(sk.data(), which ? rb_.kb : rb_.ka, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, stream_));
+  CK(cudaMemcpyAsync(sv.data(), which ? rb_.vb : rb_.va, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, stream_));
+  CK(cudaStreamSynchronize(stream_));
+  cudaFree(xr_d);
+  size_t m = 0;
+  for (size_t i = 0; i < n; ++i) cell_of[i] = raw[i] >= ncells ? -1 : (int64_t)raw[i];
+  for (size_t k = 0; k < n; ++k)
+    if (sk[k] < ncells) order[m++] = (int64_t)sv[k];
+  *n_order = m;
+  // the device upload used the sort buffers: the next step rebuilds anyway
+  return RP_OK;
+}
+
+}  // namespace rp

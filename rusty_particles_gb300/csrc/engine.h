@@ -1,0 +1,107 @@
+// Host engine behind the C ABI: owns the particle store, the device buffers
+// and the step sequencing. Mirrors the reference's `Simulation` struct
+// (src/simulation.rs:16-51) with GPU-resident state.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/rp.h"
+#include "rp_device.cuh"
+#include "rp_launch.h"
+
+namespace rp {
+
+struct HostParticle {
+  double x[3], v[3], a[3], w[3], tau[3], xres[3], vres[3], wres[3];
+  double r, m;
+  uint8_t fixed;
+  uint32_t tag;
+};
+
+struct Totals {
+  uint64_t steps = 0, removed = 0, rebuilds = 0, overlap_steps = 0, status = 0, max_count = 0;
+};
+
+class Engine {
+ public:
+  Engine(double dt, const double mn[3], const double mx[3], size_t capacity);
+  ~Engine();
+
+  // configuration (src/simulation.rs:62-91 defaults)
+  double dt;
+  double bmin[3], bmax[3];
+  int periodic[3] = {0, 0, 0};
+  Material pm{1e7, 0.3, 2500.0, 0.5, 0.5, 0.0};
+  Material wm{1e9, 0.3, 7800.0, 0.5, 0.5, 0.0};
+  int nmodel = RP_NORMAL_HERTZ, tmodel = RP_TANGENTIAL_MINDLIN;
+  int mode = RP_MODE_PARITY, prec = RP_PREC_FP64;
+  double gravity[3] = {0.0, -9.81, 0.0};
+  double href = 1.0;
+  double skin_user = -1.0;
+  int debug = 0;
+
+  int add_particle(const double x[3], double r, double m, int fixed);
+  int add_triangles(size_t n, const float* v, const float* nrm);
+  int enable_gpu(int device);
+  int step(uint64_t n);
+  size_t count();
+  int get_vec(size_t id, int which, double out[3]);
+  int set_vec(size_t id, int which, const double in[3]);
+  int read_state(rp_state* st);
+  int write_state(const rp_state* st);
+  int stats(rp_stats* st);
+  int debug_forces(double* F, double* T);
+  int debug_pairs(int64_t* pi, int64_t* pj, int32_t* visits, size_t capacity, size_t* n);
+  int debug_reference_grid(double h, int64_t* cell_of, int64_t* order, size_t* n_order, int32_t dims[3]);
+  int write_vtk(const char* path);
+  void config_changed() { dev_valid_ = false; }  // forces a fresh upload before the next step
+
+ private:
+  std::vector<HostParticle> hp_;  // id order when host_valid_
+  bool host_valid_ = true, dev_valid_ = false;
+  uint32_t next_tag_ = 0;
+  std::vector<float> tri_v_, tri_n_;
+  double ms_total_ = 0.0;
+
+  // device
+  bool gpu_ = false;
+  int device_ = -1;
+  cudaStream_t stream_ = nullptr;
+  cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+  size_t n_alloc_ = 0;  // slots allocated
+  int cap_ = 0;         // neighbour list capacity per slot
+  int n_ = 0;           // slots in use
+  Bank bank_[2] = {};
+  Ctrl* ctrl_ = nullptr;
+  Ctrl* ctrl_h_ = nullptr;  // pinned mirror
+  Ctrl last_ = {};
+  Totals tot_;
+  RebuildBufs rb_ = {};
+  uint32_t* kraw_ = nullptr;
+  size_t fcells_alloc_ = 0;
+  double* dbgF_ = nullptr;
+  double* dbgT_ = nullptr;
+  uint8_t* dbgMult_ = nullptr;
+  double* ke_ = nullptr;
+  TriRec* tri_d_ = nullptr;
+  uint32_t *tstart_d_ = nullptr, *titems_d_ = nullptr;
+  StepParams P_ = {};
+  std::vector<unsigned char> stage_;  // host staging
+
+  int ensure_gpu();
+  int upload();
+  int download();
+  int alloc_slots(size_t n);
+  int alloc_lists(int cap, bool keep_current);
+  int build_params();
+  int build_triangle_grid(double rmax);
+  void free_device();
+  int launch_steps(uint64_t n, bool resume_first);
+  int sync_ctrl();
+  int finish_step_accounting();
+};
+
+}  // namespace rp

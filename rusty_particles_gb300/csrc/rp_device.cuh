@@ -1,0 +1,184 @@
+// Device-side data layout and parameters of the DEM step.
+//
+// Particles live in HBM as structure-of-arrays in "slots": after each
+// neighbour-list rebuild the slots are re-ordered by fine cell, so particles
+// that interact sit close together in memory. Every per-slot array exists in
+// two banks; a rebuild gathers bank b into bank 1-b and flips `Ctrl::bank`,
+// so no kernel ever reads a slot another thread is writing.
+//
+// Each 32-byte record packs what one gather needs (x,y,z,radius), (v,mass),
+// (omega, reference-grid cell code): a neighbour costs three aligned 32-byte
+// sectors.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace rp {
+
+struct alignas(32) D4 {
+  double x, y, z, w;
+};
+
+enum : uint32_t { PF_FIXED = 1u, PF_DEAD = 2u };
+
+enum : unsigned { ST_OVERLAP = 1u, ST_NAN = 2u, ST_NLIST_GROW = 4u };
+
+// Device control block: written by kernels, read by the host after a chunk.
+struct Ctrl {
+  int bank;                       // bank holding the current state
+  int rebuild;                    // rebuild requested for the current step
+  int halt;                       // set when a list outgrew its capacity; later kernels of the chunk no-op
+  int overlap_flag;               // overlap > 20 % seen in the current step
+  unsigned int status;            // sticky ST_* bits
+  unsigned int max_count;         // longest neighbour list seen by the last build
+  unsigned long long removed;     // slots marked dead since the last compaction
+  unsigned long long steps_done;  // completed steps
+  unsigned long long rebuilds;    // completed list rebuilds
+  unsigned long long overlap_steps;
+};
+
+struct Material {
+  double E, nu, rho, mu, e, gamma;
+};
+
+struct Bank {
+  D4* xr;    // position, radius
+  D4* vm;    // velocity, mass
+  D4* wc;    // angular velocity, reference-grid cell code (bit pattern in .w)
+  D4* acc;   // acceleration
+  D4* tq;    // torque
+  D4* xres;  // Kahan residuals (src/particle.rs:12-18)
+  D4* vres;
+  D4* wres;
+  uint32_t* flags;  // PF_*
+  uint32_t* tag;    // insertion number (stable identity)
+  float4* xref;     // position at the last list build (.w unused)
+  uint32_t* nbr;    // neighbour rows, cap entries per slot
+  uint32_t* ncnt;   // row lengths
+  double* hist;     // physical-mode tangential spring per row entry: 3 planes of N*cap
+};
+
+// Triangle record with the per-triangle constants of src/mesh.rs:45-62
+// precomputed (same operations, so the values are bit-identical).
+struct TriRec {
+  double v0[3], e0[3], e1[3], n[3];
+  double a, b, c, det, denom, pad;
+};
+
+struct StepParams {
+  int n;  // slots
+  int cap;
+  int nmodel, tmodel, mode, prec;
+  int periodic[3];
+  int debug;
+  double dt;
+  double bmin[3], bmax[3], bsize[3];
+  double gravity[3];
+  Material pm, wm;
+  double es_pp, es_pw, gs_pp;  // effective moduli (particle-particle, particle-wall)
+  double gamma_pp, gamma_pw;   // combined surface energies
+  double beta_abs;             // |ln e / sqrt(ln^2 e + pi^2)| of the particle restitution (host libm)
+  // reference grid (parity-mode visit rule)
+  double href;
+  int rdims[3];
+  // fine grid (neighbour search)
+  double fmin[3], fcell[3];
+  int fdims[3];
+  uint32_t fncells;
+  double skin;
+  float list_scale;  // 1 + relative margin of the FP32 list test
+  // triangles
+  int ntri;
+  const TriRec* tri;
+  double tmin[3], tcell;
+  int tdims[3];
+  const uint32_t* tstart;
+  const uint32_t* titems;
+  // diagnostics
+  double* dbgF;
+  double* dbgT;
+  uint8_t* dbgMult;
+  Ctrl* ctrl;
+  Bank bank[2];
+};
+
+// ---- non-contracted double arithmetic (matches the oracle's rounding) ----
+__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+
+// Rust `as i32` from a float: saturating, NaN -> 0.
+__device__ __forceinline__ int32_t sat_i32(double f) {
+  if (f != f) return 0;
+  if (f <= -2147483648.0) return INT32_MIN;
+  if (f >= 2147483647.0) return INT32_MAX;
+  return (int32_t)f;
+}
+
+// Reference-grid coordinates packed into 63 bits (21 bits per axis, signed,
+// saturated at +-(2^20-1); dims are capped below that on the host so the
+// saturation never changes a visit decision).
+__device__ __forceinline__ unsigned long long pack_code(int32_t cx, int32_t cy, int32_t cz) {
+  const int32_t L = (1 << 20) - 1;
+  cx = cx < -L ? -L : (cx > L ? L : cx);
+  cy = cy < -L ? -L : (cy > L ? L : cy);
+  cz = cz < -L ? -L : (cz > L ? L : cz);
+  return ((unsigned long long)(uint32_t)(cx & 0x1FFFFF)) | ((unsigned long long)(uint32_t)(cy & 0x1FFFFF) << 21) |
+         ((unsigned long long)(uint32_t)(cz & 0x1FFFFF) << 42);
+}
+__device__ __forceinline__ int32_t code_axis(unsigned long long c, int k) {
+  int32_t v = (int32_t)((c >> (21 * k)) & 0x1FFFFF);
+  return (v << 11) >> 11;  // sign-extend 21 bits
+}
+
+// Reference cell coordinates of a position (src/grid.rs:30-32).
+__device__ __forceinline__ void ref_coords(const StepParams& P, double x, double y, double z, int32_t c[3]) {
+  c[0] = sat_i32(floor(dsub(x, P.bmin[0]) / P.href));
+  c[1] = sat_i32(floor(dsub(y, P.bmin[1]) / P.href));
+  c[2] = sat_i32(floor(dsub(z, P.bmin[2]) / P.href));
+}
+
+// Number of times the reference's 27-cell loop (src/grid.rs:54-85) lists the
+// cell of a particle with coordinates cj when centred on ci; 0 when cj is
+// outside the grid (the particle was never inserted, src/grid.rs:34-37).
+__device__ __forceinline__ int ref_visits(const StepParams& P, unsigned long long ci, unsigned long long cj) {
+  int m = 1;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    int32_t a = code_axis(ci, k), b = code_axis(cj, k), D = P.rdims[k];
+    if (b < 0 || b >= D) return 0;
+    int mk = 0;
+#pragma unroll
+    for (int d = -1; d <= 1; ++d) {
+      int32_t q = a + d;
+      if (P.periodic[k]) {
+        if (q < 0) q += D;
+        else if (q >= D) q -= D;
+      }
+      mk += (q == b) ? 1 : 0;
+    }
+    m *= mk;
+    if (m == 0) return 0;
+  }
+  return m;
+}
+
+// Fine-grid cell of a position: periodic axes wrap, open axes clamp.
+__device__ __forceinline__ uint32_t fine_cell(const StepParams& P, double x, double y, double z) {
+  double p[3] = {x, y, z};
+  int c[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    double q = p[k] - P.fmin[k];
+    if (P.periodic[k]) {
+      double L = P.bsize[k];
+      q = q - floor(q / L) * L;
+    }
+    double f = floor(q / P.fcell[k]);
+    int ck = (f != f) ? 0 : (f < 0.0 ? 0 : (f >= (double)P.fdims[k] ? P.fdims[k] - 1 : (int)f));
+    c[k] = ck;
+  }
+  return (uint32_t)c[0] + (uint32_t)P.fdims[0] * ((uint32_t)c[1] + (uint32_t)P.fdims[1] * (uint32_t)c[2]);
+}
+
+}  // namespace rp

@@ -1,0 +1,47 @@
+// Host-side launch interface of the device kernels (one header for the
+// translation units that launch and the engine that sequences them).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "rp_device.cuh"
+
+namespace rp {
+
+inline int grid_for(uint64_t n, int block) {
+  uint64_t g = (n + block - 1) / block;
+  const uint64_t cap = 152ull * 64ull;  // 152 SMs; grid-stride loops cover the rest
+  if (g < 1) g = 1;
+  if (g > cap) g = cap;
+  return (int)g;
+}
+
+struct RebuildBufs {
+  uint32_t *ka, *va, *kb, *vb;  // sort ping-pong
+  uint32_t* hist;               // radix digit histograms
+  uint32_t* part;               // scan partials
+  uint32_t *cstart, *cend;      // fine-cell bounds
+  int key_bits;
+  int carry_history;
+};
+
+// k_broadphase.cu
+void launch_exclusive_scan(const Ctrl* gate, const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* part,
+                           uint32_t* total, cudaStream_t s);
+uint32_t scan_parts_needed(uint32_t n);
+uint32_t radix_hist_needed(uint32_t n);
+int launch_radix_sort(const Ctrl* gate, uint32_t* ka, uint32_t* va, uint32_t* kb, uint32_t* vb, uint32_t n, int bits,
+                      uint32_t* hist, uint32_t* part, cudaStream_t s);
+void launch_rebuild(const StepParams& P, const RebuildBufs& R, cudaStream_t s);
+int launch_reference_grid(const StepParams& P, const D4* xr, int n, uint32_t ncells, int key_bits, uint32_t* kraw,
+                          uint32_t* ka, uint32_t* va, uint32_t* kb, uint32_t* vb, uint32_t* hist, uint32_t* part,
+                          cudaStream_t s);
+
+// k_step.cu
+void launch_first_half(const StepParams& P, cudaStream_t s);
+void launch_force(const StepParams& P, cudaStream_t s);
+void launch_end_step(const StepParams& P, cudaStream_t s);
+// Kinetic energy (translational + rotational) of the live slots, FP64.
+void launch_kinetic_energy(const StepParams& P, double* out, cudaStream_t s);
+
+}  // namespace rp

@@ -1,0 +1,85 @@
+"""The reference's integration tests (pydem/*.py) against the CUDA product
+through its drop-in Python surface, with the reference's own tolerances."""
+import pytest
+
+from tests import scenarios
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def rp():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import rusty_particles_gb300 as m
+    return m
+
+
+@pytest.fixture(params=["fp64", "mixed"])
+def create(rp, request):
+    prec = request.param
+
+    def make(*args):
+        s = rp.Simulation.create(*args)
+        s.set_precision(prec)
+        return s
+
+    return make
+
+
+def test_free_fall(rp):
+    scenarios.free_fall(rp.Simulation.create)
+
+
+def test_hertzian_compression(create):
+    scenarios.hertzian_compression(create)
+
+
+def test_rolling_time(create, tmp_path):
+    scenarios.rolling(create, str(tmp_path))
+
+
+def test_jkr_pull_off(create):
+    scenarios.jkr_pull_off(create)
+
+
+def test_sjkr_pull_off(create):
+    scenarios.sjkr_pull_off(create)
+
+
+def test_contact_models(rp):
+    assert scenarios.contact_models(rp.Simulation.create, pytest.raises) == 0
+
+
+def test_periodic(rp, oracle_mod):
+    g = scenarios.periodic_y(rp.Simulation.create)
+    o = scenarios.periodic_y(lambda *a: oracle_mod.OracleSimulation.create(*a, prec=64))
+    assert g.get_particle_count() == o.get_particle_count()
+
+
+def test_column_1000(rp, oracle_mod):
+    g = scenarios.column_1000(rp.Simulation.create)
+    o = scenarios.column_1000(lambda *a: oracle_mod.OracleSimulation.create(*a, prec=64))
+    assert g.get_particle_count() == o.get_particle_count()
+
+
+def test_enable_gpu_then_getters_are_current(rp):
+    # the reference's GPU mode never syncs its getters (src/simulation.rs:156-171);
+    # here they always read the current device state
+    s = rp.Simulation.create(1e-4, -1.0, -1.0, -1.0, 1.0, 1.0, 1.0, 1)
+    s.add_particle(0.0, 0.5, 0.0, 0.05, 1.0)
+    s.enable_gpu()
+    s.run(0.01)
+    _, y, _ = s.get_particle_position(0)
+    assert y < 0.5
+
+
+def test_vtk_after_steps(rp, tmp_path):
+    s = rp.Simulation.create(1e-4, -1.0, -1.0, -1.0, 1.0, 1.0, 1.0, 2)
+    s.add_particle(0.0, 0.5, 0.0, 0.05, 1.0)
+    s.add_particle(0.3, 0.5, 0.0, 0.05, 1.0)
+    s.run(0.01)
+    p = tmp_path / "a.vtk"
+    s.write_vtk(str(p))
+    assert "POINTS 2 float" in p.read_text()

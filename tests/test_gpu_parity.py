@@ -1,0 +1,181 @@
+"""GPU parity: the CUDA step against the FP64 oracle from the same state.
+
+Bars (from the reference's own decisions and the stated tolerances):
+  * reference-grid cell of every particle and the stable cell order: bit-exact
+  * contact-pair multiset (i, j, visits) of a step: bit-exact
+  * positions after a step: bit-exact (first half + drift is the same FP64
+    arithmetic without fused multiply-adds)
+  * per-particle force/torque of a step: |dF_i| <= 1e-9 * sum_j |f_ij|, the
+    scale at which summing the same contributions in another order differs
+"""
+import numpy as np
+import pytest
+
+from tests import parity_util as pu
+
+pytestmark = pytest.mark.gpu
+
+FTOL = 1e-9
+
+
+@pytest.fixture(scope="module")
+def rp():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import rusty_particles_gb300 as m
+    return m
+
+
+def one_step(rp, oracle_mod, st, normal, tangential, lo=(-0.3, -0.3, -0.3), hi=(0.3, 0.3, 0.3), dt=1e-5,
+             periodic=(False, False, False), mode=0, tris=None, cell=1.0, material=(1e7, 0.3, 2500.0, 0.5, 0.5, 0.0),
+             wall=None):
+    o = pu.oracle_sim(oracle_mod, st, dt, lo, hi, normal, tangential, periodic, mode, material, wall, tris, cell)
+    g = pu.gpu_sim(rp, st, dt, lo, hi, normal, tangential, periodic, mode, material, wall, tris, cell)
+    o.step()
+    g.step()
+    return o, g
+
+
+def compare_step(o, g, check_pairs=True):
+    assert g.get_particle_count() == o.get_particle_count()
+    so, sg = o.state(), g.get_state()
+    np.testing.assert_array_equal(sg["position"], so["x"])
+    if check_pairs:
+        assert pu.pair_counter_gpu(g) == pu.pair_counter_oracle(o)
+    Fo, To = o.last_forces()
+    Fg, Tg = g.debug_forces()
+    FS, TS = o.last_force_scale()
+    tiny = 1e-300
+    ef = np.linalg.norm(Fg - Fo, axis=1) / np.maximum(FS, tiny)
+    et = np.linalg.norm(Tg - To, axis=1) / np.maximum(TS, tiny)
+    ef[FS == 0] = np.linalg.norm(Fg - Fo, axis=1)[FS == 0]
+    et[TS == 0] = np.linalg.norm(Tg - To, axis=1)[TS == 0]
+    assert np.all(np.isfinite(Fg) == np.isfinite(Fo))
+    fin = np.isfinite(Fo).all(axis=1)
+    assert float(np.max(ef[fin], initial=0)) <= FTOL, float(np.max(ef[fin]))
+    assert float(np.max(et[fin], initial=0)) <= FTOL, float(np.max(et[fin]))
+    # velocities follow from the forces: a += F/m then a half kick
+    dv = np.abs(sg["velocity"] - so["v"])
+    assert float(np.max(dv, initial=0)) <= 1e-9 * max(1.0, float(np.max(np.abs(so["v"]), initial=0)))
+    return float(np.max(ef[fin], initial=0))
+
+
+@pytest.mark.parametrize("h", [1.0, 0.05, 0.013])
+@pytest.mark.parametrize("periodic", [(False, False, False), (True, False, True)])
+def test_reference_grid_bit_exact(rp, oracle_mod, h, periodic):
+    st = pu.random_bed(11, 3000, (-0.3, -0.3, -0.3), (0.3, 0.3, 0.3), 0.005, 0.01, outside=50)
+    lo, hi = (-0.3, -0.3, -0.3), (0.3, 0.3, 0.3)
+    o, g = one_step(rp, oracle_mod, st, 1, 0, lo, hi, periodic=periodic, cell=1.0)
+    o.set_cell_size(h)
+    do, co, oo = o.grid(now=True)
+    dg, cg, og = g.debug_reference_grid(h)
+    assert tuple(dg) == tuple(do)
+    np.testing.assert_array_equal(cg, co)
+    np.testing.assert_array_equal(og, oo)
+
+
+@pytest.mark.parametrize("normal", [0, 1, 2, 3, 4])
+@pytest.mark.parametrize("tangential", [0, 1, 2])
+def test_one_step_models(rp, oracle_mod, normal, tangential):
+    st = pu.random_bed(100 + normal * 3 + tangential, 2000, (-0.25, -0.25, -0.25), (0.25, 0.25, 0.25), 0.008, 0.012,
+                       fixed_frac=0.05)
+    gamma = 0.05 if normal in (3, 4) else 0.0
+    o, g = one_step(rp, oracle_mod, st, normal, tangential, material=(1e7, 0.3, 2500.0, 0.5, 0.5, gamma))
+    compare_step(o, g)
+
+
+@pytest.mark.parametrize("periodic", [(True, False, False), (False, True, False), (True, True, True)])
+def test_one_step_periodic(rp, oracle_mod, periodic):
+    # a box whose periodic size is not a whole number of reference cells, with
+    # particles drifting across the faces during the step
+    lo, hi = (-0.45, -0.45, -0.45), (0.45, 0.45, 0.45)
+    st = pu.random_bed(7, 4000, lo, hi, 0.008, 0.012, vscale=2.0)
+    o, g = one_step(rp, oracle_mod, st, 1, 0, lo, hi, periodic=periodic, dt=1e-3)
+    compare_step(o, g)
+
+
+def test_one_step_small_periodic_box_double_visits(rp, oracle_mod):
+    # size 0.9 with cell 1.0: dims = 2 per axis, so a periodic axis lists a
+    # neighbour cell twice and the reference counts those contacts twice
+    lo, hi = (-0.45, -0.45, -0.45), (0.45, 0.45, 0.45)
+    st = pu.random_bed(8, 1500, lo, hi, 0.01, 0.015)
+    o, g = one_step(rp, oracle_mod, st, 1, 0, lo, hi, periodic=(True, True, False))
+    pc = pu.pair_counter_oracle(o)
+    assert max(pc.values()) >= 2
+    compare_step(o, g)
+
+
+def test_one_step_walls(rp, oracle_mod):
+    from tests.stl_util import box_tris
+    lo, hi = (-0.2, -0.2, -0.2), (0.2, 0.2, 0.2)
+    tris = box_tris((-0.19, -0.19, -0.19), (0.19, 0.19, 0.19))
+    v = np.array([np.concatenate(t) for t in tris], np.float32).astype(np.float64)
+    n = np.array([np.cross(t[1] - t[0], t[2] - t[0]) / np.linalg.norm(np.cross(t[1] - t[0], t[2] - t[0]))
+                  for t in tris], np.float32).astype(np.float64)
+    st = pu.random_bed(21, 3000, lo, hi, 0.008, 0.012)
+    for nm in (1, 0, 3):
+        o, g = one_step(rp, oracle_mod, st, nm, 0, lo, hi, tris=(v, n),
+                        material=(1e7, 0.3, 2500.0, 0.5, 0.5, 0.02), wall=(1e8, 0.25, 7800.0, 0.3, 0.6, 0.01))
+        compare_step(o, g)
+
+
+def test_one_step_physical_mindlin(rp, oracle_mod):
+    lo, hi = (-0.25, -0.25, -0.25), (0.25, 0.25, 0.25)
+    st = pu.random_bed(31, 2000, lo, hi, 0.008, 0.012)
+    o, g = one_step(rp, oracle_mod, st, 1, 2, lo, hi, mode=1)
+    compare_step(o, g)
+    # history carried into the next steps
+    for _ in range(5):
+        o.step()
+        g.step()
+    so, sg = o.state(), g.get_state()
+    assert np.max(np.abs(sg["position"] - so["x"])) < 1e-12
+
+
+def test_many_steps_stay_close(rp, oracle_mod):
+    lo, hi = (-0.2, -0.2, -0.2), (0.2, 0.2, 0.2)
+    st = pu.random_bed(41, 1000, lo, hi, 0.008, 0.012)
+    o, g = one_step(rp, oracle_mod, st, 1, 0, lo, hi, dt=1e-5)
+    o.steps(199)
+    g.steps(199)
+    so, sg = o.state(), g.get_state()
+    assert np.max(np.abs(sg["position"] - so["x"])) < 1e-10
+    assert np.max(np.abs(sg["velocity"] - so["v"])) < 1e-7
+
+
+def test_removal_and_reindex(rp, oracle_mod):
+    # particles thrown out of the box are removed and ids shift down
+    # (src/simulation.rs:200-219)
+    lo, hi = (-0.2, -0.2, -0.2), (0.2, 0.2, 0.2)
+    st = pu.random_bed(51, 500, lo, hi, 0.008, 0.012)
+    st["velocity"][::7] = np.array([0.0, -400.0, 0.0])
+    o, g = one_step(rp, oracle_mod, st, 1, 0, lo, hi, dt=1e-3)
+    for _ in range(3):
+        o.step()
+        g.step()
+    assert g.get_particle_count() == o.get_particle_count() < 500
+    so, sg = o.state(), g.get_state()
+    np.testing.assert_array_equal(sg["radius"], so["r"])
+    assert np.max(np.abs(sg["position"] - so["x"])) < 1e-12
+
+
+def test_neighbour_list_growth(rp, oracle_mod):
+    # a dense cluster overflows the initial list capacity; the step halts,
+    # grows the lists and finishes with the same result
+    lo, hi = (-0.2, -0.2, -0.2), (0.2, 0.2, 0.2)
+    rng = np.random.default_rng(5)
+    n = 600
+    st = {
+        "position": rng.uniform(-0.03, 0.03, (n, 3)),
+        "radius": np.full(n, 0.01),
+        "mass": np.full(n, 1e-2),
+        "velocity": np.zeros((n, 3)),
+        "angular_velocity": np.zeros((n, 3)),
+        "acceleration": np.zeros((n, 3)),
+        "torque": np.zeros((n, 3)),
+        "fixed": np.zeros(n, np.uint8),
+    }
+    o, g = one_step(rp, oracle_mod, st, 1, 0, lo, hi, dt=1e-7)
+    assert g.stats()["status_bits"] & 4
+    compare_step(o, g)
