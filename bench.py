@@ -1,0 +1,516 @@
+#!/usr/bin/env python
+"""Benchmark of the DEM step: particle-steps/s on one GB300.
+
+Default workload (the configuration the metric is quoted on): 1,048,576
+polydisperse spheres (radii lognormal, median 2 mm, sigma 0.25, clipped to
+[1, 4] mm) packed to solid fraction ~0.55 inside a procedurally tessellated
+conical hopper of 20,000 triangles (half-angle 30 deg, outlet radius 10 median
+radii) above a floor at y = 0, periodic in x and z, Hertz + Mindlin, FP64,
+dt = 2e-6 s. The packing is a seeded FCC start relaxed by grow-and-settle
+stages run on the product engine before timing (not timed).
+
+`value` is device time over the timed steps (inputs resident in HBM; the
+state is larger than L2 so every step streams it from HBM). `e2e` is the
+same metric through the public API with host buffers: state upload, K steps
+and state read-back inside the timed region. `--impl reference` times the
+reference algorithm on the host cores (the oracle's restatement of
+`step_cpu`, literal 1 m grid and every-triangle wall loop, all threads) on a
+bounded sample of the same workload.
+
+Multi-GPU: the step does not shard (one bed per device); `--gpus N` under
+torchrun runs one independent replica per rank (weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s on 1 GB300, plain vs learned-JKR/batched/FP32, at stated force error"
+UNIT = "particle-steps/s"
+# Algorithmic bytes per particle-step of the FP64 step: read own x, v, omega
+# (72 B) + radius, mass (16 B), write x, v, omega (72 B).
+B0_FP64 = 160.0
+# Mindlin tangential spring (physical mode): 24 B read + written per pair.
+B_HIST_PAIR = 48.0
+B_TRIANGLE = 72.0
+
+
+# ----------------------------------------------------------------- workloads
+def cone_triangles(r_out, y_out, height, half_angle_deg, n_theta, n_y):
+    """Frustum wall y in [y_out, y_out+height], radius r_out + (y-y_out) tan(a),
+    n_theta x n_y quads split into 2 triangles, normals pointing inward."""
+    t = math.tan(math.radians(half_angle_deg))
+    th = np.linspace(0.0, 2.0 * np.pi, n_theta + 1)
+    ys = np.linspace(y_out, y_out + height, n_y + 1)
+    tris = []
+    for j in range(n_y):
+        y0, y1 = ys[j], ys[j + 1]
+        r0, r1 = r_out + (y0 - y_out) * t, r_out + (y1 - y_out) * t
+        for i in range(n_theta):
+            a0, a1 = th[i], th[i + 1]
+            p00 = (r0 * math.cos(a0), y0, r0 * math.sin(a0))
+            p01 = (r0 * math.cos(a1), y0, r0 * math.sin(a1))
+            p10 = (r1 * math.cos(a0), y1, r1 * math.sin(a0))
+            p11 = (r1 * math.cos(a1), y1, r1 * math.sin(a1))
+            tris.append((p00, p10, p01))
+            tris.append((p01, p10, p11))
+    v = np.asarray(tris, np.float64).reshape(-1, 9)
+    a, b, c = v[:, 0:3], v[:, 3:6], v[:, 6:9]
+    n = np.cross(b - a, c - a)
+    n /= np.linalg.norm(n, axis=1, keepdims=True)
+    centre = (a + b + c) / 3.0
+    inward = np.stack([-centre[:, 0], np.zeros(len(v)), -centre[:, 2]], 1)
+    flip = (n * inward).sum(1) < 0
+    v[flip] = np.concatenate([a[flip], c[flip], b[flip]], 1)
+    n[flip] = -n[flip]
+    return v.astype(np.float32), n.astype(np.float32)
+
+
+def floor_triangles(lo, hi, y=0.0):
+    x0, z0, x1, z1 = lo[0], lo[2], hi[0], hi[2]
+    v = np.array([[x0, y, z0, x0, y, z1, x1, y, z0], [x1, y, z0, x0, y, z1, x1, y, z1]], np.float32)
+    n = np.array([[0, 1, 0], [0, 1, 0]], np.float32)
+    return v, n
+
+
+def hopper_workload(n=1_048_576, seed=2026, phi=0.55):
+    """Hopper bed (see module docstring). Returns a dict with bounds, mesh and
+    an FCC start state (radii at full size; overlaps removed by `relax`)."""
+    rng = np.random.default_rng(seed)
+    r = np.clip(rng.lognormal(np.log(2e-3), 0.25, n), 1e-3, 4e-3)
+    rho = 2500.0
+    v_bed = float((4.0 / 3.0 * np.pi * r ** 3).sum()) / phi
+    t30 = math.tan(math.radians(30.0))
+    r_out, y_out = 10 * 2e-3, 0.15
+
+    def frustum(h):
+        R = r_out + h * t30
+        return math.pi / 3.0 * h * (R * R + R * r_out + r_out * r_out)
+
+    lo_h, hi_h = 0.0, 5.0
+    for _ in range(80):
+        mid = 0.5 * (lo_h + hi_h)
+        lo_h, hi_h = (mid, hi_h) if frustum(mid) < v_bed else (lo_h, mid)
+    h_fill = hi_h
+    h_cone = h_fill * 1.15 + 0.02
+    R_top = r_out + h_cone * t30
+    half = round(R_top + 0.05, 2)
+    lo = (-half, 0.0, -half)
+    hi = (half, round(y_out + h_cone + 0.1, 2), half)
+    # FCC sites at the bed's number density inside the cone (margin from wall)
+    a = (4.0 * v_bed / n) ** (1.0 / 3.0)
+    margin = 2e-3
+    for _ in range(20):
+        k = np.arange(-math.ceil(R_top / a) - 1, math.ceil(R_top / a) + 2)
+        ky = np.arange(0, math.ceil(h_cone / a) + 1)
+        base = np.stack(np.meshgrid(k, ky, k, indexing="ij"), -1).reshape(-1, 3).astype(np.float64)
+        offs = np.array([[0, 0, 0], [0.5, 0.5, 0], [0.5, 0, 0.5], [0, 0.5, 0.5]])
+        sites = (base[:, None, :] + offs[None]).reshape(-1, 3) * a
+        sites[:, 1] += y_out + margin
+        rho_s = np.hypot(sites[:, 0], sites[:, 2])
+        inside = (rho_s < r_out + (sites[:, 1] - y_out) * t30 - margin) & (sites[:, 1] < y_out + h_cone - margin)
+        sites = sites[inside]
+        if len(sites) >= n:
+            break
+        a *= 0.98
+    sites = sites[np.argsort(sites[:, 1], kind="stable")][:n]
+    x = sites + rng.uniform(-0.02, 0.02, sites.shape) * a
+    cv, cn = cone_triangles(r_out, y_out, h_cone, 30.0, 100, 100)
+    fv, fn = floor_triangles(lo, hi)
+    return {
+        "name": "hopper-1M",
+        "lo": lo, "hi": hi, "periodic": (True, False, True),
+        "dt": 2e-6, "normal": "hertz", "tangential": "mindlin",
+        "material": (1e7, 0.3, rho, 0.5, 0.5, 0.0),
+        "tri_v": np.concatenate([fv, cv]), "tri_n": np.concatenate([fn, cn]),
+        "position": x, "radius": r, "mass": rho * 4.0 / 3.0 * np.pi * r ** 3,
+        "describe": (f"{n:,} spheres, radii lognormal (median 2 mm, sigma 0.25, clipped [1,4] mm), solid fraction "
+                     f"{phi} in a 30-deg conical hopper (outlet radius 20 mm, {len(cv):,} triangles) over a floor, "
+                     "periodic x/z, Hertz+Mindlin, dt=2e-6 s"),
+    }
+
+
+def box_workload(seed=7):
+    """1,000 spheres on a jittered 10x10x10 lattice in [-1,1]^3 (spacing 0.2,
+    jitter <= 0.05), radii U[0.01, 0.02], reflecting walls as a 12-triangle box
+    mesh, Hertz+Coulomb, E=1e7, nu=0.3, rho=2500, e=0.5, mu=0.5, dt=1e-5."""
+    rng = np.random.default_rng(seed)
+    g = np.stack(np.meshgrid(*[np.arange(10)] * 3, indexing="ij"), -1).reshape(-1, 3)
+    x = -0.9 + 0.2 * g + rng.uniform(-0.05, 0.05, g.shape)
+    r = rng.uniform(0.01, 0.02, len(x))
+    from tests.stl_util import box_tris
+    tris = box_tris((-1, -1, -1), (1, 1, 1))
+    v = np.array([np.concatenate(t) for t in tris], np.float32)
+    n = np.array([np.cross(t[1] - t[0], t[2] - t[0]) / np.linalg.norm(np.cross(t[1] - t[0], t[2] - t[0]))
+                  for t in tris], np.float32)
+    return {
+        "name": "box-1k", "lo": (-1.0, -1.0, -1.0), "hi": (1.0, 1.0, 1.0), "periodic": (False, False, False),
+        "dt": 1e-5, "normal": "hertz", "tangential": "coulomb", "material": (1e7, 0.3, 2500.0, 0.5, 0.5, 0.0),
+        "tri_v": v, "tri_n": n, "position": x, "radius": r, "mass": 2500.0 * 4.0 / 3.0 * np.pi * r ** 3,
+        "describe": "1,000 spheres, jittered 10^3 lattice in [-1,1]^3, radii U[0.01,0.02], 12-triangle box walls, "
+                    "Hertz+Coulomb, dt=1e-5 s",
+    }
+
+
+def make_sim(rp, wl, mode="parity", precision="fp64"):
+    lo, hi = wl["lo"], wl["hi"]
+    s = rp.Simulation.create(wl["dt"], lo[0], lo[1], lo[2], hi[0], hi[1], hi[2], len(wl["radius"]))
+    s.set_interaction_mode(mode)
+    s.set_precision(precision)
+    s.set_particle_material(*wl["material"])
+    s.set_contact_models(wl["normal"], wl["tangential"])
+    s.set_periodic_boundary(*wl["periodic"])
+    s.add_triangles(wl["tri_v"], wl["tri_n"])
+    s.add_particles(wl["position"], wl["radius"], wl["mass"])
+    return s
+
+
+def relax(rp, wl, stages=9, steps_per_stage=100, settle=300, log=None):
+    """Grow radii from 0.6x to 1x in stages while a damped, frictionless,
+    gravity-free run removes the overlaps; updates wl["position"] in place."""
+    x = wl["position"].copy()
+    r, m = wl["radius"], wl["mass"]
+    lo, hi = wl["lo"], wl["hi"]
+    s = rp.Simulation.create(1e-5, lo[0], lo[1], lo[2], hi[0], hi[1], hi[2], len(r))
+    s.set_interaction_mode("parity")
+    s.set_particle_material(1e7, 0.3, 2500.0, 0.0, 0.05, 0.0)
+    s.set_contact_models("hertz", "coulomb")
+    s.set_periodic_boundary(*wl["periodic"])
+    s.set_gravity(0.0, 0.0, 0.0)
+    s.add_triangles(wl["tri_v"], wl["tri_n"])
+    s.add_particles(x, r * 0.6, m * 0.216)
+    t0 = time.time()
+    for k, f in enumerate(np.linspace(0.6, 1.0, stages)):
+        st = {"radius": r * f, "mass": m * f ** 3, "velocity": np.zeros_like(x), "angular_velocity": np.zeros_like(x),
+              "acceleration": np.zeros_like(x), "torque": np.zeros_like(x)}
+        s.set_state(st)
+        s.steps(steps_per_stage if k < stages - 1 else settle)
+    out = s.get_state()
+    if len(out["radius"]) != len(r):
+        raise RuntimeError(f"relaxation lost particles ({len(out['radius'])} of {len(r)})")
+    wl["position"] = out["position"]
+    if log:
+        log(f"relaxed {len(r):,} particles in {time.time() - t0:.1f} s")
+    return wl
+
+
+# ------------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi samples (200 ms) while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [q.strip() for q in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, p[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- helpers
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def init_dist(ws):
+    if ws <= 1:
+        return None
+    import torch.distributed as dist
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    dist.init_process_group("gloo")
+    return dist
+
+
+def allreduce_max(dist, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([float(v)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def allreduce_sum(dist, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([float(v)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profiled_traffic(workload_name, n):
+    """DRAM bytes per force-kernel launch from the committed ncu summary
+    (profiles/force_kernel_<workload>.json), scaled to n particles."""
+    p = os.path.join(ROOT, "profiles", f"force_kernel_{workload_name}.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["dram_bytes_per_launch"]) * n / float(d["particles"])
+    except (OSError, KeyError, ValueError):
+        return None
+
+
+# ------------------------------------------------------------ CPU baseline
+def cpu_sample(wl, n_sample, seed=3):
+    """A compact sub-block of the bed: the n_sample particles nearest the bed's
+    centre of mass, with the workload's full mesh."""
+    x = wl["position"]
+    c = x.mean(0)
+    idx = np.argsort(np.linalg.norm(x - c, axis=1), kind="stable")[:n_sample]
+    idx.sort()
+    return idx
+
+
+def run_oracle_sample(wl, idx, steps, threads):
+    from oracle import oracle as om
+    om.build()
+    if threads:
+        om.set_threads(threads)
+    lo, hi = wl["lo"], wl["hi"]
+    o = om.OracleSimulation(wl["dt"], lo, hi, prec=64)
+    o.set_mode(0)
+    o.set_options(record_pairs=False, keep_contact_map=True)
+    o.set_particle_material(*wl["material"])
+    o.set_contact_models(wl["normal"], wl["tangential"])
+    o.set_periodic_boundary(*wl["periodic"])
+    for i in idx:
+        p = wl["position"][i]
+        o.add_particle(p[0], p[1], p[2], wl["radius"][i], wl["mass"][i])
+    o.add_triangles(wl["tri_v"].astype(np.float64), wl["tri_n"].astype(np.float64))
+    o.steps(1)  # warm-up (grid, contact map, page faults)
+    t0 = time.perf_counter()
+    o.steps(steps)
+    dt = time.perf_counter() - t0
+    return len(idx) * steps / dt, dt, om.get_threads()
+
+
+def cpu_baseline(wl, budget_s=20.0, threads=0):
+    """Time the reference algorithm on a bounded sample (about budget_s of CPU work)."""
+    n_sample = min(len(wl["radius"]), 4096)
+    idx = cpu_sample(wl, n_sample)
+    rate1, t1, cores = run_oracle_sample(wl, idx, 1, threads)
+    steps = max(1, min(200, int(budget_s / max(t1, 1e-6))))
+    rate, t, cores = run_oracle_sample(wl, idx, steps, threads)
+    return {
+        "value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+        "sample": (f"{len(idx):,} particles nearest the bed centre with all {len(wl['tri_v']):,} triangles, "
+                   f"{steps} steps ({t:.1f} s); literal reference algorithm (1 m cells, every triangle per "
+                   "particle), FP64, OpenMP over particles; its per-particle cost grows with N"),
+    }
+
+
+# -------------------------------------------------------------------- arms
+def run_reference(args, log):
+    ws, rank, _ = dist_info()
+    dist = init_dist(ws)
+    if rank != 0:
+        barrier(dist)
+        return 0
+    wl = hopper_workload() if args.workload == "hopper" else box_workload()
+    threads = os.cpu_count() or 1
+    rates = []
+    from oracle import oracle as om
+    om.build()
+    om.set_threads(threads)
+    n_sample = min(len(wl["radius"]), 4096)
+    idx = cpu_sample(wl, n_sample)
+    for _ in range(max(1, args.warmup_ref)):
+        run_oracle_sample(wl, idx, 1, threads)
+    t_all = 0.0
+    for _ in range(args.steps_ref):
+        rate, t, cores = run_oracle_sample(wl, idx, 1, threads)
+        rates.append(rate)
+        t_all += t
+    value = len(idx) * len(rates) / t_all
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": len(rates),
+        "warmup": args.warmup_ref, "ms_per_step": 1e3 * t_all / len(rates), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": wl["name"], "describe": wl["describe"], "mode": "parity"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{len(idx):,} particles nearest the bed centre, all {len(wl['tri_v']):,} "
+                                   "triangles, one step per timed sample; literal reference algorithm"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    barrier(dist)
+    return 0
+
+
+def run_ours(args, log):
+    ws, rank, local = dist_info()
+    dist = init_dist(ws)
+    import torch
+    import rusty_particles_gb300 as rp
+    torch.cuda.set_device(local)
+    wl = hopper_workload() if args.workload == "hopper" else box_workload()
+    n = len(wl["radius"])
+    if args.workload == "hopper":
+        relax(rp, wl, log=log)
+    sim = make_sim(rp, wl, args.mode, args.precision)
+    sim._L.rp_enable_gpu(sim._h, local)
+    sim._L.rp_set_profiling(sim._h, 1)
+    sim.steps(args.warmup)
+    torch.cuda.synchronize()
+    s0 = sim.stats()
+    clocks = ClockSampler(local)
+    barrier(dist)
+    torch.cuda.synchronize()
+    clocks.start()
+    t0 = time.perf_counter()
+    sim.steps(args.steps)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    barrier(dist)
+    ck = clocks.stop()
+    s1 = sim.stats()
+    dev_ms = s1["device_ms"] - s0["device_ms"]
+    n_now = s1["particles"]
+    t_max = allreduce_max(dist, dev_ms)
+    total_units = allreduce_sum(dist, n_now * args.steps)
+    value = total_units / (t_max / 1e3)
+    force_ms = (s1["force_ms"] - s0["force_ms"]) / max(1, s1["force_launches"] - s0["force_launches"])
+    launches = s1["kernel_launches"] - s0["kernel_launches"]
+    # algorithmic bytes per force launch (see B0_FP64)
+    tri = len(wl["tri_v"])
+    alg_bytes = n_now * B0_FP64 + tri * B_TRIANGLE
+    peak, peak_kind = measured_peaks()
+    achieved = alg_bytes / (force_ms / 1e3) / 1e9
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": profiled_traffic(wl["name"], n_now), "kernel": "k_force", "avg_launch_ms": force_ms,
+            "algorithmic_bytes_per_launch": alg_bytes, "peak_source": peak_kind}
+    # end to end through the public API with host buffers
+    st = sim.get_state()
+    e2e_steps = args.steps
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sim.set_state(st)
+    sim.steps(e2e_steps)
+    out = sim.get_state()
+    wall_e2e = time.perf_counter() - t0
+    h2d = n * (8 * 32 + 4 + 4 + 16)
+    d2h = n * (8 * 32 + 4 + 4)
+    e2e_val = allreduce_sum(dist, n * e2e_steps) / allreduce_max(dist, wall_e2e)
+    del out
+    if rank != 0:
+        barrier(dist)
+        return 0
+    cpu = None if args.no_cpu else cpu_baseline(wl, budget_s=args.cpu_budget)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.precision == "fp64" else "f32-pairs/f64-state", "data": "synthetic",
+        "config": {"workload": wl["name"], "describe": wl["describe"], "particles": int(n_now), "mode": args.mode,
+                   "precision": args.precision, "parallelism": f"replicas x{ws}",
+                   "l2": f"inputs larger than L2 (particle state {n_now * 312 / 1e6:.0f} MB)",
+                   "wall_s_timed": wall},
+        "roofline": roof, "cpu_baseline": cpu,
+        "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d / e2e_steps,
+                "d2h_bytes_per_step": d2h / e2e_steps,
+                "note": "set_state (H2D of the full state) + steps(K) + get_state (D2H), K = steps"},
+        "gpu_launches": int(launches), "clocks": ck,
+        "stats": {k: s1[k] for k in ("neighbor_rebuilds", "max_neighbors", "neighbor_capacity", "removed")},
+    }
+    print(json.dumps(line), flush=True)
+    barrier(dist)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=500)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=["hopper", "box"], default="hopper")
+    ap.add_argument("--mode", choices=["parity", "physical"], default="parity")
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    args = ap.parse_args()
+    args.steps_ref = max(1, min(args.steps, 10))
+    args.warmup_ref = max(1, min(args.warmup, 2))
+    log = (lambda m: print(m, file=sys.stderr, flush=True))
+    if args.impl == "reference":
+        return run_reference(args, log)
+    return run_ours(args, log)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

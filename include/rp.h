@@ -89,6 +89,9 @@ typedef struct rp_stats {
   uint64_t max_neighbors;      /* longest list at the last rebuild */
   double kinetic_energy;       /* FP64, translational + rotational, at the last rp_get_stats */
   double device_ms;            /* device time of the stepping calls so far */
+  uint64_t kernel_launches;    /* kernels launched by stepping calls so far */
+  uint64_t force_launches;     /* force-kernel launches timed (profiling on) */
+  double force_ms;             /* their summed device time (CUDA events on the launching stream) */
 } rp_stats;
 
 #define RP_STATUS_OVERLAP 1u    /* overlap > 20 % of the smaller radius (src/simulation.rs:361-370) */
@@ -157,10 +160,13 @@ int rp_set_interaction_mode(rp_sim* sim, int mode);      /* RP_MODE_*; default P
 int rp_set_gravity(rp_sim* sim, double gx, double gy, double gz); /* default (0,-9.81,0), src/simulation.rs:267 */
 int rp_set_reference_cell_size(rp_sim* sim, double h);   /* default 1.0, src/simulation.rs:66 */
 int rp_set_skin(rp_sim* sim, double skin);               /* Verlet skin; <= 0 selects the default */
+int rp_set_neighbor_capacity(rp_sim* sim, int capacity); /* initial list slots per particle (grows on demand) */
 int rp_set_threads(int n);                               /* set_num_threads (src/lib.rs:15-22) */
 
 /* --- metrics and errors */
 int rp_get_stats(rp_sim* sim, rp_stats* out);
+/* Time every force-kernel launch with CUDA events (adds two event records per step). */
+int rp_set_profiling(rp_sim* sim, int enable);
 const char* rp_last_error(void);
 const char* rp_version(void);
 

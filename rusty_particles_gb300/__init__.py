@@ -199,6 +199,9 @@ class Simulation:
     def set_skin(self, skin):
         check(self._L.rp_set_skin(self._h, float(skin)))
 
+    def set_neighbor_capacity(self, cap):
+        check(self._L.rp_set_neighbor_capacity(self._h, int(cap)))
+
     def set_reference_cell_size(self, h):
         check(self._L.rp_set_reference_cell_size(self._h, float(h)))
 

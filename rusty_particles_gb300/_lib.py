@@ -58,6 +58,9 @@ class RpStats(ctypes.Structure):
         ("max_neighbors", ctypes.c_uint64),
         ("kinetic_energy", ctypes.c_double),
         ("device_ms", ctypes.c_double),
+        ("kernel_launches", ctypes.c_uint64),
+        ("force_launches", ctypes.c_uint64),
+        ("force_ms", ctypes.c_double),
     ]
 
 
@@ -94,8 +97,10 @@ SIGNATURES = {
     "rp_set_gravity": (ctypes.c_int, [ctypes.c_void_p] + [ctypes.c_double] * 3),
     "rp_set_reference_cell_size": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
     "rp_set_skin": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
+    "rp_set_neighbor_capacity": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "rp_set_threads": (ctypes.c_int, [ctypes.c_int]),
     "rp_get_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(RpStats)]),
+    "rp_set_profiling": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "rp_last_error": (ctypes.c_char_p, []),
     "rp_version": (ctypes.c_char_p, []),
     "rp_set_debug": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),

@@ -1,8 +1,10 @@
 // Host engine: particle store, device buffers and step sequencing.
 //
-// A step is launched as: first half (boundary, kick, drift) -> gated rebuild
-// chain (hash, radix sort, cell bounds, reorder, Verlet lists) -> forces +
-// second half -> end-of-step bookkeeping. Steps are issued in chunks with one
+// A step is launched as: first half (the previous step's second half kick,
+// boundary, kick, drift) -> gated rebuild chain (hash, radix sort, cell
+// bounds, reorder, Verlet lists) -> forces (a, tau only) -> end-of-step
+// bookkeeping; a stepping call ends with the pending second half kick, so the
+// state between calls is the reference's end-of-step state. Steps are issued in chunks with one
 // host synchronisation per chunk; a device control block reports completed
 // steps, rebuilds, removals and a halt when a neighbour list outgrew its
 // capacity (the engine then grows the lists and resumes the halted step).
@@ -100,10 +102,21 @@ void Engine::free_device() {
   ctrl_h_ = nullptr;
   if (ev0_) cudaEventDestroy(ev0_);
   if (ev1_) cudaEventDestroy(ev1_);
+  for (cudaEvent_t e : fev_) cudaEventDestroy(e);
+  fev_.clear();
   if (stream_) cudaStreamDestroy(stream_);
   stream_ = nullptr;
   ev0_ = ev1_ = nullptr;
   gpu_ = false;
+}
+
+void Engine::free_lists() {
+  if (!gpu_) return;
+  for (int b = 0; b < 2; ++b) {
+    dfree(bank_[b].nbr);
+    dfree(bank_[b].hist);
+  }
+  dfree(dbgMult_);
 }
 
 int Engine::ensure_gpu() {
@@ -580,18 +593,30 @@ int Engine::finish_step_accounting() {
   return RP_OK;
 }
 
-int Engine::launch_steps(uint64_t n, bool) {
+// Steps are issued with the second half kick of each step fused into the
+// next step's first-half kernel; the caller completes the last one.
+int Engine::launch_steps(uint64_t n, bool pending_half) {
   const uint64_t CHUNK = 512;
+  if (profiling && fev_.size() < 2 * CHUNK) {
+    while (fev_.size() < 2 * CHUNK) {
+      cudaEvent_t e;
+      CK(cudaEventCreate(&e));
+      fev_.push_back(e);
+    }
+  }
   uint64_t remaining = n;
   while (remaining > 0) {
     const uint64_t chunk = std::min(remaining, CHUNK);
     const uint64_t before = last_.steps_done;
     CK(cudaEventRecord(ev0_, stream_));
     for (uint64_t s = 0; s < chunk; ++s) {
-      launch_first_half(P_, stream_);
-      launch_rebuild(P_, rb_, stream_);
-      launch_force(P_, stream_);
-      launch_end_step(P_, stream_);
+      launches_ += launch_first_half(P_, pending_half, stream_);
+      pending_half = true;
+      launches_ += launch_rebuild(P_, rb_, stream_);
+      if (profiling) CK(cudaEventRecord(fev_[2 * s], stream_));
+      launches_ += launch_force(P_, stream_);
+      if (profiling) CK(cudaEventRecord(fev_[2 * s + 1], stream_));
+      launches_ += launch_end_step(P_, stream_);
     }
     CK(cudaEventRecord(ev1_, stream_));
     CK(cudaGetLastError());
@@ -599,6 +624,15 @@ int Engine::launch_steps(uint64_t n, bool) {
     float ms = 0.f;
     cudaEventElapsedTime(&ms, ev0_, ev1_);
     ms_total_ += ms;
+    if (profiling) {
+      for (uint64_t s = 0; s < chunk; ++s) {
+        float fm = 0.f;
+        if (cudaEventElapsedTime(&fm, fev_[2 * s], fev_[2 * s + 1]) == cudaSuccess) {
+          force_ms_ += fm;
+          force_launches_ += 1;
+        }
+      }
+    }
     while (ctrl_h_->halt) {
       // A list outgrew its capacity during the rebuild of the step after
       // `steps_done`: grow the lists (keeping the current bank's rows for the
@@ -615,9 +649,9 @@ int Engine::launch_steps(uint64_t n, bool) {
       CK(cudaMemcpyAsync(&ctrl_->halt, &zero, sizeof(int), cudaMemcpyHostToDevice, stream_));
       CK(cudaMemcpyAsync(&ctrl_->max_count, &zu, sizeof(unsigned), cudaMemcpyHostToDevice, stream_));
       CK(cudaStreamSynchronize(stream_));
-      launch_rebuild(P_, rb_, stream_);
-      launch_force(P_, stream_);
-      launch_end_step(P_, stream_);
+      launches_ += launch_rebuild(P_, rb_, stream_);
+      launches_ += launch_force(P_, stream_);
+      launches_ += launch_end_step(P_, stream_);
       CK(cudaGetLastError());
       TRY(sync_ctrl());
     }
@@ -646,6 +680,9 @@ int Engine::step(uint64_t n) {
   host_valid_ = false;
   int r = launch_steps(n, false);
   if (r != RP_OK) return r;
+  launches_ += launch_second_half(P_, stream_);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(stream_));
   // many removals: compact through the host before the next step
   if (last_.removed > 0 && last_.removed * 8 > (uint64_t)n_) {
     TRY(download());
@@ -727,6 +764,9 @@ int Engine::stats(rp_stats* s) {
   s->neighbor_capacity = (uint64_t)cap_;
   s->max_neighbors = tot_.max_count;
   s->device_ms = ms_total_;
+  s->kernel_launches = launches_;
+  s->force_launches = force_launches_;
+  s->force_ms = force_ms_;
   if (gpu_ && dev_valid_ && n_ > 0) {
     CK(cudaSetDevice(device_));
     launch_kinetic_energy(P_, ke_, stream_);

@@ -42,6 +42,7 @@ class Engine {
   double href = 1.0;
   double skin_user = -1.0;
   int debug = 0;
+  int profiling = 0;
 
   int add_particle(const double x[3], double r, double m, int fixed);
   int add_triangles(size_t n, const float* v, const float* nrm);
@@ -58,6 +59,12 @@ class Engine {
   int debug_reference_grid(double h, int64_t* cell_of, int64_t* order, size_t* n_order, int32_t dims[3]);
   int write_vtk(const char* path);
   void config_changed() { dev_valid_ = false; }  // forces a fresh upload before the next step
+  void set_capacity(int c) {
+    if (!host_valid_) download();
+    free_lists();
+    cap_ = c;
+    dev_valid_ = false;
+  }
 
  private:
   std::vector<HostParticle> hp_;  // id order when host_valid_
@@ -65,6 +72,10 @@ class Engine {
   uint32_t next_tag_ = 0;
   std::vector<float> tri_v_, tri_n_;
   double ms_total_ = 0.0;
+  uint64_t launches_ = 0;
+  uint64_t force_launches_ = 0;
+  double force_ms_ = 0.0;
+  std::vector<cudaEvent_t> fev_;  // force-kernel event pairs (profiling)
 
   // device
   bool gpu_ = false;
@@ -99,6 +110,7 @@ class Engine {
   int build_params();
   int build_triangle_grid(double rmax);
   void free_device();
+  void free_lists();
   int launch_steps(uint64_t n, bool resume_first);
   int sync_ctrl();
   int finish_step_accounting();

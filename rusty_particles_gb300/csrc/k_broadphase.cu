@@ -400,8 +400,9 @@ __global__ void k_rebuild_finish(StepParams P) {
 
 // Old-list slots are indexed by old slot numbers, so the history lookup in
 // k_build_nlist needs perm (new slot -> old slot) for both ends of a pair.
-void launch_rebuild(const StepParams& P, const RebuildBufs& R, cudaStream_t s) {
+int launch_rebuild(const StepParams& P, const RebuildBufs& R, cudaStream_t s) {
   const Ctrl* g = P.ctrl;
+  const int passes = (R.key_bits + 7) / 8 < 1 ? 1 : (R.key_bits + 7) / 8;
   const int nb = grid_for(P.n, 256);
   k_hash_fine<<<nb, 256, 0, s>>>(P, R.ka, R.va);
   int which = launch_radix_sort(g, R.ka, R.va, R.kb, R.vb, (uint32_t)P.n, R.key_bits, R.hist, R.part, s);
@@ -412,6 +413,7 @@ void launch_rebuild(const StepParams& P, const RebuildBufs& R, cudaStream_t s) {
   k_reorder<<<nb, 256, 0, s>>>(P, sv);
   k_build_nlist<<<grid_for(P.n, 128), 128, 0, s>>>(P, R.cstart, R.cend, sv, R.carry_history);
   k_rebuild_finish<<<1, 1, 0, s>>>(P);
+  return 1 + 5 * passes + 5;
 }
 
 // Diagnostic: the reference grid's key per slot (written to kraw) and the

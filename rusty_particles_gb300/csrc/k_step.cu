@@ -144,12 +144,34 @@ __device__ __forceinline__ V spring_coulomb(double fn, V rv, V n, V& xi, double 
   return trial;
 }
 
+// Second half of velocity Verlet for one particle (src/simulation.rs:541-561):
+// Kahan-compensated v += a dt/2 and omega += (tau/I) dt/2, I = 0.4 m r^2.
+__device__ __forceinline__ void second_half_kick(V& v, V& vres, V& w, V& wres, V a, V tau, double m, double r,
+                                                 double dt) {
+  V dv = (0.5 * a) * dt;
+  V yv = dv - vres;
+  V tv = v + yv;
+  vres = (tv - v) - yv;
+  v = tv;
+  double inertia = 0.4 * m * r * r;
+  V aa = tau / inertia;
+  V dw = (0.5 * aa) * dt;
+  V yw = dw - wres;
+  V tw = w + yw;
+  wres = (tw - w) - yw;
+  w = tw;
+}
+
 // ------------------------------------------------------------- first half
-// src/simulation.rs:176-263: periodic wrap, out-of-bounds removal (marked
-// dead here, compacted by the host later; removal does not change any other
-// particle's first half), Kahan-compensated half kick + drift + angular half
+// The force kernel only writes a and tau: neighbours read v and omega while
+// it runs, so the second half kick of step n-1 is applied here, at the start
+// of step n (FUSE), and by k_second_half at the end of a stepping call.
+// Then src/simulation.rs:176-263: periodic wrap, out-of-bounds removal
+// (marked dead here and compacted by the host later; removal changes no other
+// particle's update), Kahan-compensated half kick + drift + angular half
 // kick. Also records the reference-grid cell code and requests a list
 // rebuild when a particle moved more than half the skin since the last build.
+template <bool FUSE>
 __global__ void __launch_bounds__(256) k_first_half(StepParams P) {
   Ctrl* C = P.ctrl;
   if (C->halt) return;
@@ -161,8 +183,18 @@ __global__ void __launch_bounds__(256) k_first_half(StepParams P) {
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < P.n; k += gridDim.x * blockDim.x) {
     uint32_t fl = B.flags[k];
     if (fl & PF_DEAD) continue;
-    D4 xr = B.xr[k];
-    V x = xyz(xr);
+    D4 xr = B.xr[k], vm = B.vm[k], wc = B.wc[k];
+    V x = xyz(xr), v = xyz(vm), w = xyz(wc);
+    const bool moving = !(fl & PF_FIXED);
+    V a = vmk(0.0, 0.0, 0.0), tau = a, vres = a, wres = a, xres = a;
+    if (moving) {
+      a = xyz(B.acc[k]);
+      tau = xyz(B.tq[k]);
+      vres = xyz(B.vres[k]);
+      wres = xyz(B.wres[k]);
+      xres = xyz(B.xres[k]);
+      if (FUSE) second_half_kick(v, vres, w, wres, a, tau, vm.w, xr.w, dt);
+    }
     if (anyp) {
       if (P.periodic[0]) { if (x.x < P.bmin[0]) x.x = x.x + P.bsize[0]; else if (x.x >= P.bmax[0]) x.x = x.x - P.bsize[0]; }
       if (P.periodic[1]) { if (x.y < P.bmin[1]) x.y = x.y + P.bsize[1]; else if (x.y >= P.bmax[1]) x.y = x.y - P.bsize[1]; }
@@ -179,11 +211,7 @@ __global__ void __launch_bounds__(256) k_first_half(StepParams P) {
       atomicAdd(&C->removed, 1ull);
       continue;
     }
-    D4 wc = B.wc[k];
-    if (!(fl & PF_FIXED)) {
-      D4 vm = B.vm[k];
-      V v = xyz(vm), a = xyz(B.acc[k]);
-      V vres = xyz(B.vres[k]), xres = xyz(B.xres[k]);
+    if (moving) {
       V dv = (0.5 * a) * dt;
       V yv = dv - vres;
       V tv = v + yv;
@@ -195,8 +223,7 @@ __global__ void __launch_bounds__(256) k_first_half(StepParams P) {
       xres = (tx - x) - yx;
       x = tx;
       double inertia = 0.4 * vm.w * xr.w * xr.w;
-      V w = xyz(wc), wres = xyz(B.wres[k]);
-      V aa = xyz(B.tq[k]) / inertia;
+      V aa = tau / inertia;
       V dw = (0.5 * aa) * dt;
       V yw = dw - wres;
       V tw = w + yw;
@@ -224,6 +251,24 @@ __global__ void __launch_bounds__(256) k_first_half(StepParams P) {
     if (!(d2 <= half_skin * half_skin)) want_rebuild = true;  // NaN (no build yet) also rebuilds
   }
   if (want_rebuild) C->rebuild = 1;
+}
+
+// Completes the last step of a stepping call (the pending second half).
+__global__ void __launch_bounds__(256) k_second_half(StepParams P) {
+  Ctrl* C = P.ctrl;
+  if (C->halt) return;
+  const Bank B = P.bank[C->bank];
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < P.n; k += gridDim.x * blockDim.x) {
+    uint32_t fl = B.flags[k];
+    if (fl & (PF_DEAD | PF_FIXED)) continue;
+    D4 xr = B.xr[k], vm = B.vm[k], wc = B.wc[k];
+    V v = xyz(vm), w = xyz(wc), vres = xyz(B.vres[k]), wres = xyz(B.wres[k]);
+    second_half_kick(v, vres, w, wres, xyz(B.acc[k]), xyz(B.tq[k]), vm.w, xr.w, P.dt);
+    B.vm[k] = D4{v.x, v.y, v.z, vm.w};
+    B.wc[k] = D4{w.x, w.y, w.z, wc.w};
+    B.vres[k] = D4{vres.x, vres.y, vres.z, 0.0};
+    B.wres[k] = D4{wres.x, wres.y, wres.z, 0.0};
+  }
 }
 
 // ------------------------------------------------- forces + second half
@@ -394,31 +439,12 @@ __global__ void __launch_bounds__(128) k_force(StepParams P) {
       P.dbgT[3 * (size_t)k] = T.x; P.dbgT[3 * (size_t)k + 1] = T.y; P.dbgT[3 * (size_t)k + 2] = T.z;
     }
     if (!isfinite(F.x + F.y + F.z + T.x + T.y + T.z)) atomicOr(&C->status, (unsigned)ST_NAN);
-    // apply + second half (src/simulation.rs:532-561)
+    // apply (src/simulation.rs:532-536); the second half kick of this step
+    // runs in the next k_first_half or in k_second_half
     const V a = vmk(P.gravity[0], P.gravity[1], P.gravity[2]) + F / mi;
     const V tau = vmk(0.0, 0.0, 0.0) + T;
     B.acc[k] = D4{a.x, a.y, a.z, 0.0};
     B.tq[k] = D4{tau.x, tau.y, tau.z, 0.0};
-    if (!(fl & PF_FIXED)) {
-      V v = vi, vres = xyz(B.vres[k]);
-      V dv = (0.5 * a) * dt;
-      V yv = dv - vres;
-      V tv = v + yv;
-      vres = (tv - v) - yv;
-      v = tv;
-      double inertia = 0.4 * mi * ri * ri;
-      V w = wi, wres = xyz(B.wres[k]);
-      V aa = tau / inertia;
-      V dw = (0.5 * aa) * dt;
-      V yw = dw - wres;
-      V tw = w + yw;
-      wres = (tw - w) - yw;
-      w = tw;
-      B.vm[k] = D4{v.x, v.y, v.z, mi};
-      B.vres[k] = D4{vres.x, vres.y, vres.z, 0.0};
-      B.wc[k] = D4{w.x, w.y, w.z, wi4.w};
-      B.wres[k] = D4{wres.x, wres.y, wres.z, 0.0};
-    }
   }
   if (excess) C->overlap_flag = 1;
 }
@@ -447,21 +473,33 @@ __global__ void k_kinetic(StepParams P, double* out) {
   if ((threadIdx.x & 31) == 0) atomicAdd(out, e);
 }
 
-void launch_first_half(const StepParams& P, cudaStream_t s) {
-  if (P.n == 0) return;
-  k_first_half<<<grid_for(P.n, 256), 256, 0, s>>>(P);
+int launch_first_half(const StepParams& P, bool fuse_second_half, cudaStream_t s) {
+  if (P.n == 0) return 0;
+  if (fuse_second_half) k_first_half<true><<<grid_for(P.n, 256), 256, 0, s>>>(P);
+  else k_first_half<false><<<grid_for(P.n, 256), 256, 0, s>>>(P);
+  return 1;
 }
 
-void launch_force(const StepParams& P, cudaStream_t s) {
-  if (P.n == 0) return;
+int launch_second_half(const StepParams& P, cudaStream_t s) {
+  if (P.n == 0) return 0;
+  k_second_half<<<grid_for(P.n, 256), 256, 0, s>>>(P);
+  return 1;
+}
+
+int launch_force(const StepParams& P, cudaStream_t s) {
+  if (P.n == 0) return 0;
   const int g = grid_for(P.n, 128);
   const bool hist = P.mode == 1 && P.tmodel != 0;
   if (P.mode == 0) k_force<false, false><<<g, 128, 0, s>>>(P);
   else if (hist) k_force<true, true><<<g, 128, 0, s>>>(P);
   else k_force<true, false><<<g, 128, 0, s>>>(P);
+  return 1;
 }
 
-void launch_end_step(const StepParams& P, cudaStream_t s) { k_end_step<<<1, 1, 0, s>>>(P); }
+int launch_end_step(const StepParams& P, cudaStream_t s) {
+  k_end_step<<<1, 1, 0, s>>>(P);
+  return 1;
+}
 
 void launch_kinetic_energy(const StepParams& P, double* out, cudaStream_t s) {
   cudaMemsetAsync(out, 0, sizeof(double), s);

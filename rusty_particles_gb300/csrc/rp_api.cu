@@ -450,6 +450,16 @@ int rp_set_skin(rp_sim* s, double skin) {
   return RP_OK;
 }
 
+int rp_set_neighbor_capacity(rp_sim* s, int capacity) {
+  SIM_OR_FAIL(s);
+  if (capacity < 1 || capacity > 4096) {
+    set_error("neighbour capacity must be in [1, 4096]");
+    return RP_E_INVALID_ARG;
+  }
+  s->e->set_capacity(capacity);
+  return RP_OK;
+}
+
 static int g_threads_set = 0;
 int rp_set_threads(int n) {
   // The reference sizes rayon's global pool once (src/lib.rs:15-22); a second
@@ -473,6 +483,12 @@ int rp_get_stats(rp_sim* s, rp_stats* out) {
     return RP_E_INVALID_ARG;
   }
   return s->e->stats(out);
+}
+
+int rp_set_profiling(rp_sim* s, int enable) {
+  SIM_OR_FAIL(s);
+  s->e->profiling = enable != 0;
+  return RP_OK;
 }
 
 const char* rp_last_error(void) { return rp::g_err.c_str(); }

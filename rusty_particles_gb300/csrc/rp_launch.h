@@ -32,15 +32,16 @@ uint32_t scan_parts_needed(uint32_t n);
 uint32_t radix_hist_needed(uint32_t n);
 int launch_radix_sort(const Ctrl* gate, uint32_t* ka, uint32_t* va, uint32_t* kb, uint32_t* vb, uint32_t n, int bits,
                       uint32_t* hist, uint32_t* part, cudaStream_t s);
-void launch_rebuild(const StepParams& P, const RebuildBufs& R, cudaStream_t s);
+int launch_rebuild(const StepParams& P, const RebuildBufs& R, cudaStream_t s);  // returns kernels launched
 int launch_reference_grid(const StepParams& P, const D4* xr, int n, uint32_t ncells, int key_bits, uint32_t* kraw,
                           uint32_t* ka, uint32_t* va, uint32_t* kb, uint32_t* vb, uint32_t* hist, uint32_t* part,
                           cudaStream_t s);
 
 // k_step.cu
-void launch_first_half(const StepParams& P, cudaStream_t s);
-void launch_force(const StepParams& P, cudaStream_t s);
-void launch_end_step(const StepParams& P, cudaStream_t s);
+int launch_first_half(const StepParams& P, bool fuse_second_half, cudaStream_t s);  // each returns kernels launched
+int launch_second_half(const StepParams& P, cudaStream_t s);
+int launch_force(const StepParams& P, cudaStream_t s);
+int launch_end_step(const StepParams& P, cudaStream_t s);
 // Kinetic energy (translational + rotational) of the live slots, FP64.
 void launch_kinetic_energy(const StepParams& P, double* out, cudaStream_t s);
 

@@ -15,10 +15,13 @@ def random_bed(seed, n, lo, hi, rmin, rmax, vscale=0.05, wscale=1.0, ascale=1.0,
     rng = np.random.default_rng(seed)
     lo = np.asarray(lo, float)
     hi = np.asarray(hi, float)
-    spacing = 2.0 * rmax * 0.985
-    dims = np.maximum(((hi - lo) / spacing).astype(int), 1)
+    # per-axis spacing that divides the box exactly, so a periodic face is
+    # seamless; sites fill the box from the bottom (y) up, as a settled bed
+    s0 = rmin + rmax  # about half of the neighbour pairs overlap
+    dims = np.maximum(np.ceil((hi - lo) / s0).astype(int), 1)
+    spacing = (hi - lo) / dims
     g = np.stack(np.meshgrid(*[np.arange(d) for d in dims], indexing="ij"), -1).reshape(-1, 3)
-    rng.shuffle(g)
+    g = g[np.lexsort((g[:, 2], g[:, 0], g[:, 1]))]
     g = g[:n]
     x = lo + (g + 0.5) * spacing + rng.uniform(-0.02, 0.02, g.shape) * rmax
     k = len(x)
