@@ -161,6 +161,10 @@ int rp_set_gravity(rp_sim* sim, double gx, double gy, double gz); /* default (0,
 int rp_set_reference_cell_size(rp_sim* sim, double h);   /* default 1.0, src/simulation.rs:66 */
 int rp_set_skin(rp_sim* sim, double skin);               /* Verlet skin; <= 0 selects the default */
 int rp_set_neighbor_capacity(rp_sim* sim, int capacity); /* initial list slots per particle (grows on demand) */
+/* 1 (default): a stepping call is one CUDA-graph launch whose device-side loop
+ * runs all steps and rebuilds lists only when needed; 0: the host issues the
+ * kernels step by step in chunks. */
+int rp_set_device_loop(rp_sim* sim, int enable);
 int rp_set_threads(int n);                               /* set_num_threads (src/lib.rs:15-22) */
 
 /* --- metrics and errors */

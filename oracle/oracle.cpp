@@ -551,7 +551,7 @@ struct Sim : Base {
     V3<T> tc = ra.cross(fc);
     ttot += tc;
     fs += (double)fc.length();
-    ts += (double)tc.length();
+    ts += (double)p.r * (double)fc.length();  // |r_a| |f|: the rounding scale of r_a x f
     return true;
   }
 
@@ -679,7 +679,7 @@ struct Sim : Base {
         V3<T> tc = ra.cross(fc);
         ttot += tc;
         fs += (double)fc.length();
-        ts += (double)tc.length();
+        ts += (double)p.r * (double)fc.length();
       }
       lastF[i] = ftot;
       lastT[i] = ttot;

@@ -87,10 +87,14 @@ Engine::~Engine() { free_device(); }
 void Engine::free_device() {
   if (!gpu_) return;
   cudaSetDevice(device_);
+  destroy_graph();
+  if (cap_stream_) cudaStreamDestroy(cap_stream_);
+  if (cap_stream2_) cudaStreamDestroy(cap_stream2_);
+  cap_stream_ = cap_stream2_ = nullptr;
   for (int b = 0; b < 2; ++b) {
     Bank& B = bank_[b];
     dfree(B.xr); dfree(B.vm); dfree(B.wc); dfree(B.acc); dfree(B.tq);
-    dfree(B.xres); dfree(B.vres); dfree(B.wres); dfree(B.flags); dfree(B.tag); dfree(B.xref);
+    dfree(B.xres); dfree(B.vres); dfree(B.wres); dfree(B.flags); dfree(B.tag); dfree(B.xref); dfree(B.xf);
     dfree(B.nbr); dfree(B.ncnt); dfree(B.hist);
   }
   dfree(rb_.ka); dfree(rb_.va); dfree(rb_.kb); dfree(rb_.vb); dfree(rb_.hist); dfree(rb_.part);
@@ -209,6 +213,7 @@ int Engine::alloc_slots(size_t n) {
     TRY(dalloc(&B.xr, na)); TRY(dalloc(&B.vm, na)); TRY(dalloc(&B.wc, na)); TRY(dalloc(&B.acc, na));
     TRY(dalloc(&B.tq, na)); TRY(dalloc(&B.xres, na)); TRY(dalloc(&B.vres, na)); TRY(dalloc(&B.wres, na));
     TRY(dalloc(&B.flags, na)); TRY(dalloc(&B.tag, na)); TRY(dalloc(&B.xref, na)); TRY(dalloc(&B.ncnt, na));
+    TRY(dalloc(&B.xf, na));
   }
   TRY(dalloc(&rb_.ka, na)); TRY(dalloc(&rb_.va, na)); TRY(dalloc(&rb_.kb, na)); TRY(dalloc(&rb_.vb, na));
   TRY(dalloc(&kraw_, na));
@@ -264,6 +269,7 @@ int Engine::alloc_lists(int cap, bool keep_current) {
     dfree(dbgMult_);
   }
   cap_ = cap;
+  graph_dirty_ = true;
   return RP_OK;
 }
 
@@ -318,6 +324,18 @@ int Engine::build_params() {
   if (!(skin > 0.0)) skin = 1e-6;
   P.skin = skin;
   P.list_scale = 1.0f + 1e-5f;
+  {
+    double cutmax = 2.0 * rmax * adh;
+    double lm = 0.0;
+    bool ok = true;
+    for (int k = 0; k < 3; ++k)
+      if (periodic[k]) {
+        lm = std::max(lm, P.bsize[k]);
+        if (P.bsize[k] < 4.0 * cutmax) ok = false;
+      }
+    P.pretest = ok ? 1 : 0;
+    P.lmax = (float)lm;
+  }
   double h = 2.0 * rmax * adh + skin;
   if (!(h > 0.0)) h = 1.0;
   const uint64_t max_cells = std::max<uint64_t>(4ull * (uint64_t)n_ + (1ull << 16), 1ull << 20);
@@ -506,6 +524,9 @@ int Engine::upload() {
     CK(cudaMemcpy(B.tag, tags.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice));
     std::vector<float4> xref(n, make_float4(NAN, NAN, NAN, 0.f));
     CK(cudaMemcpy(B.xref, xref.data(), sizeof(float4) * n, cudaMemcpyHostToDevice));
+    for (size_t i = 0; i < n; ++i)
+      xref[i] = make_float4((float)hp_[i].x[0], (float)hp_[i].x[1], (float)hp_[i].x[2], (float)hp_[i].r);
+    CK(cudaMemcpy(B.xf, xref.data(), sizeof(float4) * n, cudaMemcpyHostToDevice));
   }
   for (int b = 0; b < 2; ++b) CK(cudaMemset(bank_[b].ncnt, 0, sizeof(uint32_t) * n_alloc_));
   if (need_hist)
@@ -518,6 +539,7 @@ int Engine::upload() {
   CK(cudaMemcpy(ctrl_, &c, sizeof(Ctrl), cudaMemcpyHostToDevice));
   last_ = c;
   dev_valid_ = true;
+  graph_dirty_ = true;  // kernel parameters changed
   return RP_OK;
 }
 
@@ -593,9 +615,136 @@ int Engine::finish_step_accounting() {
   return RP_OK;
 }
 
-// Steps are issued with the second half kick of each step fused into the
-// next step's first-half kernel; the caller completes the last one.
-int Engine::launch_steps(uint64_t n, bool pending_half) {
+// A list outgrew its capacity during the rebuild of the step after
+// `steps_done` (that step's first half already ran): grow the lists, keeping
+// the current bank's rows for the history carry-over, and finish that step.
+int Engine::recover_halt() {
+  while (ctrl_h_->halt) {
+    int newcap = std::max<int>(cap_ + 8, (int)(ctrl_h_->max_count * 5 / 4 + 8));
+    TRY(alloc_lists(newcap, true));
+    P_.cap = cap_;
+    P_.bank[0] = bank_[0];
+    P_.bank[1] = bank_[1];
+    P_.dbgMult = dbgMult_;
+    graph_dirty_ = true;
+    tot_.status |= ST_NLIST_GROW;
+    int zero = 0;
+    unsigned zu = 0;
+    CK(cudaMemcpyAsync(&ctrl_->halt, &zero, sizeof(int), cudaMemcpyHostToDevice, stream_));
+    CK(cudaMemcpyAsync(&ctrl_->max_count, &zu, sizeof(unsigned), cudaMemcpyHostToDevice, stream_));
+    CK(cudaStreamSynchronize(stream_));
+    launches_ += launch_rebuild(P_, rb_, stream_);
+    launches_ += launch_force(P_, stream_);
+    launches_ += launch_end_step(P_, stream_);
+    CK(cudaGetLastError());
+    TRY(sync_ctrl());
+  }
+  return RP_OK;
+}
+
+void Engine::destroy_graph() {
+  if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
+  if (graph_) cudaGraphDestroy(graph_);
+  graph_exec_ = nullptr;
+  graph_ = nullptr;
+}
+
+// The device step loop: a WHILE node whose body is one step (first half,
+// rebuild condition, IF node holding the rebuild chain, forces, end of
+// step). k_end_step sets the loop condition from the device counters, so a
+// stepping call of any length is one graph launch and the host never has to
+// decide whether a step needs a rebuild.
+int Engine::build_graph() {
+  destroy_graph();
+  if (!cap_stream_) {
+    CK(cudaStreamCreateWithFlags(&cap_stream_, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&cap_stream2_, cudaStreamNonBlocking));
+  }
+  cudaGraph_t g = nullptr;
+  CK(cudaGraphCreate(&g, 0));
+  graph_ = g;
+  cudaGraphConditionalHandle hloop;
+  CK(cudaGraphConditionalHandleCreate(&hloop, g, 1, cudaGraphCondAssignDefault));
+  cudaGraphNodeParams wp = {};
+  wp.type = cudaGraphNodeTypeConditional;
+  wp.conditional.handle = hloop;
+  wp.conditional.type = cudaGraphCondTypeWhile;
+  wp.conditional.size = 1;
+  cudaGraphNode_t wnode;
+  CK(cudaGraphAddNode(&wnode, g, nullptr, nullptr, 0, &wp));
+  cudaGraph_t body = wp.conditional.phGraph_out[0];
+  cudaGraphConditionalHandle hif;
+  CK(cudaGraphConditionalHandleCreate(&hif, body, 0, cudaGraphCondAssignDefault));
+  CK(cudaStreamBeginCaptureToGraph(cap_stream_, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+  launch_first_half(P_, cap_stream_);
+  launch_rebuild_condition(P_, hif, cap_stream_);
+  cudaStreamCaptureStatus st;
+  cudaGraph_t cg = nullptr;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t nd = 0;
+  CK(cudaStreamGetCaptureInfo(cap_stream_, &st, nullptr, &cg, &deps, nullptr, &nd));
+  cudaGraphNodeParams ip = {};
+  ip.type = cudaGraphNodeTypeConditional;
+  ip.conditional.handle = hif;
+  ip.conditional.type = cudaGraphCondTypeIf;
+  ip.conditional.size = 1;
+  cudaGraphNode_t inode;
+  CK(cudaGraphAddNode(&inode, cg, deps, nullptr, nd, &ip));
+  CK(cudaStreamUpdateCaptureDependencies(cap_stream_, &inode, nullptr, 1, cudaStreamSetCaptureDependencies));
+  CK(cudaStreamBeginCaptureToGraph(cap_stream2_, ip.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                   cudaStreamCaptureModeRelaxed));
+  chain_kernels_ = launch_rebuild(P_, rb_, cap_stream2_);
+  cudaGraph_t t2 = nullptr;
+  CK(cudaStreamEndCapture(cap_stream2_, &t2));
+  launch_force(P_, cap_stream_);
+  launch_end_step_loop(P_, hloop, cap_stream_);
+  cudaGraph_t t1 = nullptr;
+  CK(cudaStreamEndCapture(cap_stream_, &t1));
+  CK(cudaGraphInstantiate(&graph_exec_, g, 0));
+  graph_dirty_ = false;
+  return RP_OK;
+}
+
+int Engine::launch_steps_graph(uint64_t n) {
+  if (graph_dirty_ || !graph_exec_) {
+    int r = build_graph();
+    if (r != RP_OK) {
+      // conditional graph nodes unavailable: fall back to host-issued steps
+      destroy_graph();
+      use_graph_ = false;
+      cudaGetLastError();
+      return launch_steps(n);
+    }
+  }
+  uint64_t remaining = n;
+  while (remaining > 0) {
+    const uint64_t before = last_.steps_done, rb_before = last_.rebuilds;
+    unsigned long long lim[2] = {before + remaining, 0ull};  // target, iters
+    CK(cudaMemcpyAsync(&ctrl_->target, &lim[0], sizeof(unsigned long long), cudaMemcpyHostToDevice, stream_));
+    CK(cudaMemcpyAsync(&ctrl_->iters, &lim[1], sizeof(unsigned long long), cudaMemcpyHostToDevice, stream_));
+    CK(cudaEventRecord(ev0_, stream_));
+    CK(cudaGraphLaunch(graph_exec_, stream_));
+    CK(cudaEventRecord(ev1_, stream_));
+    TRY(sync_ctrl());
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ev0_, ev1_);
+    ms_total_ += ms;
+    TRY(recover_halt());
+    launches_ += 4 * (ctrl_h_->steps_done - before) + (uint64_t)chain_kernels_ * (ctrl_h_->rebuilds - rb_before);
+    TRY(finish_step_accounting());
+    const uint64_t done = last_.steps_done - before;
+    if (done == 0) {
+      set_error("device step loop made no progress");
+      return RP_E_DEVICE_FLAG;
+    }
+    remaining -= std::min(done, remaining);
+  }
+  return RP_OK;
+}
+
+// Host-issued steps in chunks (used when profiling per force launch): the
+// same kernels as the device loop, every rebuild kernel gated on the device.
+int Engine::launch_steps(uint64_t n) {
   const uint64_t CHUNK = 512;
   if (profiling && fev_.size() < 2 * CHUNK) {
     while (fev_.size() < 2 * CHUNK) {
@@ -610,8 +759,7 @@ int Engine::launch_steps(uint64_t n, bool pending_half) {
     const uint64_t before = last_.steps_done;
     CK(cudaEventRecord(ev0_, stream_));
     for (uint64_t s = 0; s < chunk; ++s) {
-      launches_ += launch_first_half(P_, pending_half, stream_);
-      pending_half = true;
+      launches_ += launch_first_half(P_, stream_);
       launches_ += launch_rebuild(P_, rb_, stream_);
       if (profiling) CK(cudaEventRecord(fev_[2 * s], stream_));
       launches_ += launch_force(P_, stream_);
@@ -633,28 +781,7 @@ int Engine::launch_steps(uint64_t n, bool pending_half) {
         }
       }
     }
-    while (ctrl_h_->halt) {
-      // A list outgrew its capacity during the rebuild of the step after
-      // `steps_done`: grow the lists (keeping the current bank's rows for the
-      // history carry-over) and finish that step.
-      int newcap = std::max<int>(cap_ + 8, (int)(ctrl_h_->max_count * 5 / 4 + 8));
-      TRY(alloc_lists(newcap, true));
-      P_.cap = cap_;
-      P_.bank[0] = bank_[0];
-      P_.bank[1] = bank_[1];
-      P_.dbgMult = dbgMult_;
-      tot_.status |= ST_NLIST_GROW;
-      int zero = 0;
-      unsigned zu = 0;
-      CK(cudaMemcpyAsync(&ctrl_->halt, &zero, sizeof(int), cudaMemcpyHostToDevice, stream_));
-      CK(cudaMemcpyAsync(&ctrl_->max_count, &zu, sizeof(unsigned), cudaMemcpyHostToDevice, stream_));
-      CK(cudaStreamSynchronize(stream_));
-      launches_ += launch_rebuild(P_, rb_, stream_);
-      launches_ += launch_force(P_, stream_);
-      launches_ += launch_end_step(P_, stream_);
-      CK(cudaGetLastError());
-      TRY(sync_ctrl());
-    }
+    TRY(recover_halt());
     TRY(finish_step_accounting());
     const uint64_t done = last_.steps_done - before;
     if (done == 0) {
@@ -678,7 +805,7 @@ int Engine::step(uint64_t n) {
     return RP_OK;
   }
   host_valid_ = false;
-  int r = launch_steps(n, false);
+  int r = (use_graph_ && !profiling) ? launch_steps_graph(n) : launch_steps(n);
   if (r != RP_OK) return r;
   launches_ += launch_second_half(P_, stream_);
   CK(cudaGetLastError());

@@ -76,6 +76,17 @@ class Engine {
   uint64_t force_launches_ = 0;
   double force_ms_ = 0.0;
   std::vector<cudaEvent_t> fev_;  // force-kernel event pairs (profiling)
+  // device step loop (CUDA graph with WHILE and IF conditional nodes)
+  cudaGraph_t graph_ = nullptr;
+  cudaGraphExec_t graph_exec_ = nullptr;
+  cudaStream_t cap_stream_ = nullptr, cap_stream2_ = nullptr;
+  bool graph_dirty_ = true;
+  int chain_kernels_ = 0;
+
+ public:
+  bool use_graph_ = true;
+
+ private:
 
   // device
   bool gpu_ = false;
@@ -111,7 +122,11 @@ class Engine {
   int build_triangle_grid(double rmax);
   void free_device();
   void free_lists();
-  int launch_steps(uint64_t n, bool resume_first);
+  int launch_steps(uint64_t n);
+  int launch_steps_graph(uint64_t n);
+  int build_graph();
+  void destroy_graph();
+  int recover_halt();
   int sync_ctrl();
   int finish_step_accounting();
 };

@@ -290,6 +290,7 @@ __global__ void k_reorder(StepParams P, const uint32_t* perm) {
     D.flags[k] = S.flags[o];
     D.tag[k] = S.tag[o];
     D.xref[k] = make_float4((float)x.x, (float)x.y, (float)x.z, 0.f);
+    D.xf[k] = S.xf[o];
   }
 }
 

@@ -1,6 +1,6 @@
-// Per-step kernels of the DEM step: boundary + first half of velocity Verlet,
-// the pair/wall force gather fused with the second half, and the end-of-step
-// bookkeeping.
+// Per-step kernels of the DEM step: the first-half kernel (the previous
+// step's second half kick, boundary rule, half kick + drift), the pair/wall
+// force gather, the end-of-step bookkeeping and the closing second half kick.
 //
 // This translation unit is compiled with -fmad=false: every double operation
 // rounds exactly as the oracle's (-ffp-contract=off), so positions after the
@@ -8,6 +8,13 @@
 // bit-identical to the reference algorithm evaluated in FP64 from the same
 // state. Force magnitudes differ only where a transcendental is evaluated
 // differently (delta^1.5 as delta*sqrt(delta)), well inside 1e-9 relative.
+//
+// Precision forms of the pair force (StepParams::prec):
+//   FP64  — all pair math in double.
+//   MIXED — the cutoff decision, r_sum^2 - d^2 (the overlap without
+//           cancellation) and v_i - v_j stay in double; normals, relative
+//           velocity, force laws and torques run in float; the per-particle
+//           force/torque sums, the state and the integrator stay in double.
 #include <cfloat>
 
 #include "rp_device.cuh"
@@ -15,133 +22,236 @@
 
 namespace rp {
 
-struct V {
-  double x, y, z;
+template <typename R>
+struct T3 {
+  R x, y, z;
 };
+template <typename R> __device__ __forceinline__ T3<R> t3(R x, R y, R z) { return T3<R>{x, y, z}; }
+template <typename R> __device__ __forceinline__ T3<R> operator+(T3<R> a, T3<R> b) { return T3<R>{a.x + b.x, a.y + b.y, a.z + b.z}; }
+template <typename R> __device__ __forceinline__ T3<R> operator-(T3<R> a, T3<R> b) { return T3<R>{a.x - b.x, a.y - b.y, a.z - b.z}; }
+template <typename R> __device__ __forceinline__ T3<R> operator-(T3<R> a) { return T3<R>{-a.x, -a.y, -a.z}; }
+template <typename R> __device__ __forceinline__ T3<R> operator*(T3<R> a, R s) { return T3<R>{a.x * s, a.y * s, a.z * s}; }
+template <typename R> __device__ __forceinline__ T3<R> operator*(R s, T3<R> a) { return T3<R>{s * a.x, s * a.y, s * a.z}; }
+template <typename R> __device__ __forceinline__ T3<R> operator/(T3<R> a, R s) { return T3<R>{a.x / s, a.y / s, a.z / s}; }
+template <typename R> __device__ __forceinline__ R dot(T3<R> a, T3<R> b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+template <typename R> __device__ __forceinline__ T3<R> cross(T3<R> a, T3<R> r) {
+  return T3<R>{a.y * r.z - r.y * a.z, a.z * r.x - r.z * a.x, a.x * r.y - r.x * a.y};
+}
+template <typename R> __device__ __forceinline__ R len(T3<R> a) { return sqrt(dot(a, a)); }
+template <typename R, typename S> __device__ __forceinline__ T3<R> cvt(T3<S> a) { return T3<R>{(R)a.x, (R)a.y, (R)a.z}; }
+
+using V = T3<double>;
+using Vf = T3<float>;
 __device__ __forceinline__ V vmk(double x, double y, double z) { return V{x, y, z}; }
-__device__ __forceinline__ V operator+(V a, V b) { return V{a.x + b.x, a.y + b.y, a.z + b.z}; }
-__device__ __forceinline__ V operator-(V a, V b) { return V{a.x - b.x, a.y - b.y, a.z - b.z}; }
-__device__ __forceinline__ V operator-(V a) { return V{-a.x, -a.y, -a.z}; }
-__device__ __forceinline__ V operator*(V a, double s) { return V{a.x * s, a.y * s, a.z * s}; }
-__device__ __forceinline__ V operator*(double s, V a) { return V{s * a.x, s * a.y, s * a.z}; }
-__device__ __forceinline__ V operator/(V a, double s) { return V{a.x / s, a.y / s, a.z / s}; }
-__device__ __forceinline__ double dot(V a, V b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-__device__ __forceinline__ V cross(V a, V r) { return V{a.y * r.z - r.y * a.z, a.z * r.x - r.z * a.x, a.x * r.y - r.x * a.y}; }
-__device__ __forceinline__ double len(V a) { return sqrt(dot(a, a)); }
 __device__ __forceinline__ V xyz(const D4& d) { return V{d.x, d.y, d.z}; }
 
 constexpr double kPi = 3.14159265358979323846;
 
 // ------------------------------------------------------------- force laws
 // src/physics.rs:49-70
-__device__ __forceinline__ double lsd_mag(double overlap, double vn, double kn, double gn) {
-  return fmax(kn * overlap - gn * vn, 0.0);
+template <typename R>
+__device__ __forceinline__ R lsd_mag(R overlap, R vn, R kn, R gn) {
+  return fmax(kn * overlap - gn * vn, R(0));
 }
-// src/physics.rs:86-129 (delta^1.5 evaluated as delta*sqrt(delta))
-__device__ __forceinline__ double hertz_mag(double overlap, double vn, double es, double rs, double ms, double beta_abs) {
-  if (overlap <= 0.0) return 0.0;
-  double kn = (4.0 / 3.0) * es * sqrt(rs);
-  double fe = kn * (overlap * sqrt(overlap));
-  double kt = 2.0 * es * sqrt(rs * overlap);
-  double cn = 2.0 * sqrt(ms * kt) * beta_abs;
-  double fd = -cn * vn;
-  return fmax(fe + fd, 0.0);
+// src/physics.rs:86-129. With s = sqrt(R* delta): the elastic term
+// (4/3) E* sqrt(R*) delta^1.5 = (4/3) E* s delta and the tangent stiffness
+// 2 E* sqrt(R* delta) = 2 E* s share one square root.
+template <typename R>
+__device__ __forceinline__ R hertz_mag(R overlap, R vn, R es, R rs, R ms, R beta_abs) {
+  if (overlap <= R(0)) return R(0);
+  R s = sqrt(rs * overlap);
+  R fe = R(4.0 / 3.0) * es * s * overlap;
+  R kt = R(2) * es * s;
+  R cn = R(2) * sqrt(ms * kt) * beta_abs;
+  R fd = -cn * vn;
+  return fmax(fe + fd, R(0));
 }
-__device__ __forceinline__ double hertz_elastic_mag(double overlap, double es, double rs) {
-  double kn = (4.0 / 3.0) * es * sqrt(rs);
-  return overlap > 0.0 ? kn * (overlap * sqrt(overlap)) : 0.0;
+template <typename R>
+__device__ __forceinline__ R hertz_elastic_mag(R overlap, R es, R rs) {
+  R kn = R(4.0 / 3.0) * es * sqrt(rs);
+  return overlap > R(0) ? kn * (overlap * sqrt(overlap)) : R(0);
 }
 // src/physics.rs:132-219 (Newton on a^2/R* - sqrt(C a) - delta = 0)
-__device__ __forceinline__ double jkr_mag(double overlap, double es, double rs, double gamma) {
-  if (gamma <= 0.0) return hertz_elastic_mag(overlap, es, rs);
-  const double eight_pi = 8.0 * kPi;
-  double c_val = eight_pi * gamma / es;
-  double sqrt_c = sqrt(c_val);
-  double a = overlap > 0.0 ? sqrt(rs * overlap) : rs * 0.5;
+template <typename R>
+__device__ __forceinline__ R jkr_mag(R overlap, R es, R rs, R gamma) {
+  if (gamma <= R(0)) return hertz_elastic_mag(overlap, es, rs);
+  const R eight_pi = R(8) * R(kPi);
+  R c_val = eight_pi * gamma / es;
+  R sqrt_c = sqrt(c_val);
+  R a = overlap > R(0) ? sqrt(rs * overlap) : rs * R(0.5);
   for (int it = 0; it < 20; ++it) {
-    if (a <= 0.0) a = 1e-9;
-    double ts = sqrt(c_val * a);
-    double f_val = a * a / rs - ts - overlap;
-    double df = 2.0 * a / rs - 0.5 * sqrt_c / sqrt(a);
-    if (fabs(df) < 1e-9) break;
-    double da = f_val / df;
-    double max_step = a * 0.5;
-    double step = da;
+    if (a <= R(0)) a = R(1e-9);
+    R ts = sqrt(c_val * a);
+    R f_val = a * a / rs - ts - overlap;
+    R df = R(2) * a / rs - R(0.5) * sqrt_c / sqrt(a);
+    if (fabs(df) < R(1e-9)) break;
+    R da = f_val / df;
+    R max_step = a * R(0.5);
+    R step = da;
     if (step < -max_step) step = -max_step;
     if (step > max_step) step = max_step;
     a = a - step;
-    if (fabs(step) < 1e-6 * rs) break;
+    if (fabs(step) < R(1e-6) * rs) break;
   }
-  double ts = sqrt(c_val * a);
-  double f_val = a * a / rs - ts - overlap;
-  if (fabs(f_val) > 1e-3 * rs) return 0.0;
-  if (a <= 0.0) return 0.0;
-  double a3 = a * a * a;
-  double term1 = 4.0 * es * a3 / (3.0 * rs);
-  double term2 = sqrt(eight_pi * gamma * es * a3);
-  double fm = term1 - term2;
-  double f_pull = (-2.0 / 3.0) * kPi * gamma * rs;
-  if (fm < f_pull) return 0.0;
+  R ts = sqrt(c_val * a);
+  R f_val = a * a / rs - ts - overlap;
+  if (fabs(f_val) > R(1e-3) * rs) return R(0);
+  if (a <= R(0)) return R(0);
+  R a3 = a * a * a;
+  R term1 = R(4) * es * a3 / (R(3) * rs);
+  R term2 = sqrt(eight_pi * gamma * es * a3);
+  R fm = term1 - term2;
+  R f_pull = R(-2.0 / 3.0) * R(kPi) * gamma * rs;
+  if (fm < f_pull) return R(0);
   return fm;
 }
 // src/physics.rs:234-325
-__device__ __forceinline__ double sjkr_mag(double overlap, double vn, double es, double rs, double gamma) {
-  if (gamma <= 0.0) return hertz_elastic_mag(overlap, es, rs);
-  double f_pull = 1.5 * kPi * gamma * rs;
-  double term = 3.0 * (kPi * kPi) * (gamma * gamma) * rs / (es * es);
-  double delta_c = -sqrt(term);
-  if (overlap < delta_c) return 0.0;
-  double coh = vn > 0.0 ? 1.0 : 0.0;
-  double fh = overlap > 0.0 ? (4.0 / 3.0) * es * sqrt(rs) * (overlap * sqrt(overlap)) : 0.0;
+template <typename R>
+__device__ __forceinline__ R sjkr_mag(R overlap, R vn, R es, R rs, R gamma) {
+  if (gamma <= R(0)) return hertz_elastic_mag(overlap, es, rs);
+  R f_pull = R(1.5) * R(kPi) * gamma * rs;
+  R term = R(3) * (R(kPi) * R(kPi)) * (gamma * gamma) * rs / (es * es);
+  R delta_c = -sqrt(term);
+  if (overlap < delta_c) return R(0);
+  R coh = vn > R(0) ? R(1) : R(0);
+  R fh = overlap > R(0) ? R(4.0 / 3.0) * es * sqrt(rs) * (overlap * sqrt(overlap)) : R(0);
   return fh - coh * f_pull;
 }
 
-// Normal force vector for the configured model. `vn_src` is the relative
-// velocity the model sees (the reference passes Vec3::ZERO to the
-// hysteretic particle-particle law, src/simulation.rs:409-411).
-__device__ __forceinline__ V normal_force(int model, double overlap, V n, V rv, double es, double rs, double ms,
-                                          double beta_abs, double gamma, bool wall) {
-  double m;
+// Normal force vector for the configured model. The reference passes
+// Vec3::ZERO as the relative velocity to the hysteretic particle-particle law
+// (src/simulation.rs:409-411) and the real one for walls (:495-501).
+template <typename R>
+__device__ __forceinline__ R normal_mag(int model, R overlap, T3<R> n, T3<R> rv, R es, R rs, R ms, R beta_abs,
+                                       R gamma, bool wall) {
+  R m;
   switch (model) {
     case 1: m = hertz_mag(overlap, dot(rv, n), es, rs, ms, beta_abs); break;
     case 0: {
-      double kn = es * rs;
-      double gn = 0.5 * sqrt(ms * kn);
+      R kn = es * rs;
+      R gn = R(0.5) * sqrt(ms * kn);
       m = lsd_mag(overlap, dot(rv, n), kn, gn);
     } break;
     case 2: {
-      double kn = es * rs;
-      double vn = wall ? dot(rv, n) : dot(vmk(0.0, 0.0, 0.0), n);
-      m = lsd_mag(overlap, vn, kn, 0.0);
+      R kn = es * rs;
+      R vn = wall ? dot(rv, n) : dot(t3(R(0), R(0), R(0)), n);
+      m = lsd_mag(overlap, vn, kn, R(0));
     } break;
     case 3: m = jkr_mag(overlap, es, rs, gamma); break;
     default: m = sjkr_mag(overlap, dot(rv, n), es, rs, gamma); break;
   }
-  return m * n;
+  return m;
+}
+// The vector form, f n, as the reference returns it.
+template <typename R>
+__device__ __forceinline__ T3<R> normal_force(int model, R overlap, T3<R> n, T3<R> rv, R es, R rs, R ms, R beta_abs,
+                                              R gamma, bool wall) {
+  return normal_mag<R>(model, overlap, n, rv, es, rs, ms, beta_abs, gamma, wall) * n;
 }
 
-// src/physics.rs:385-397
-__device__ __forceinline__ V coulomb_force(double fn, V rv, V n, double mu) {
-  V vt = rv - dot(rv, n) * n;
-  if (dot(vt, vt) < 1e-8) return vmk(0.0, 0.0, 0.0);
-  double inv = 1.0 / len(vt);
-  V dir = vt * inv;
+// src/physics.rs:385-397 (direction by one reciprocal square root)
+template <typename R>
+__device__ __forceinline__ T3<R> coulomb_force(R fn, T3<R> rv, T3<R> n, R mu) {
+  T3<R> vt = rv - dot(rv, n) * n;
+  const R vt2 = dot(vt, vt);
+  if (vt2 < R(1e-8)) return t3(R(0), R(0), R(0));
+  R inv = rsqrt(vt2);
+  T3<R> dir = vt * inv;
   return (-mu * fn) * dir;
 }
 // src/physics.rs:400-434 with the spring `xi` in registers.
-__device__ __forceinline__ V spring_coulomb(double fn, V rv, V n, V& xi, double kt, double mu, double dt) {
-  V vt = rv - dot(rv, n) * n;
+template <typename R>
+__device__ __forceinline__ T3<R> spring_coulomb(R fn, T3<R> rv, T3<R> n, T3<R>& xi, R kt, R mu, R dt) {
+  T3<R> vt = rv - dot(rv, n) * n;
   xi = xi + vt * dt;
-  V trial = (-kt) * xi;
-  double tm = len(trial);
-  double fc = mu * fn;
+  T3<R> trial = (-kt) * xi;
+  R tm = len(trial);
+  R fc = mu * fn;
   if (tm > fc) {
-    V dir = tm > 1e-6 ? trial / tm : vmk(0.0, 0.0, 0.0);
-    V ft = fc * dir;
+    T3<R> dir = tm > R(1e-6) ? trial / tm : t3(R(0), R(0), R(0));
+    T3<R> ft = fc * dir;
     xi = (-ft) / kt;
     return ft;
   }
   return trial;
+}
+
+// One contact seen from particle i (src/simulation.rs:358-460), for a pair
+// that passed the cutoff test. Inputs in FP64; the law arithmetic in R.
+// Returns the contact force on i and its torque r_a x f in FP64.
+template <typename R, bool PHYS, bool HIST>
+__device__ __forceinline__ void pair_contact(const StepParams& P, V d, double d2, double rsum, double ri, double rj,
+                                             double mi, double mj, V vi, V vj, V wi, V wj, double* hist, size_t plane,
+                                             V& fc_out, V& tc_out, bool& excess) {
+  R overlap;
+  T3<R> n;
+  if (sizeof(R) == sizeof(double)) {
+    const double dist = sqrt(d2);
+    overlap = (R)(rsum - dist);
+    const double inv = 1.0 / dist;
+    const V nd = dist > 1e-6 ? d * inv : vmk(0.0, 1.0, 0.0);
+    n = cvt<R>(nd);
+  } else {
+    // overlap = (r_sum^2 - d^2) / (r_sum + d): the difference is taken in FP64
+    const float dist = sqrtf((float)d2);
+    overlap = (R)((float)(rsum * rsum - d2) / ((float)rsum + dist));
+    bool far_enough;
+    if (d2 > 1.001e-12) far_enough = true;
+    else if (d2 < 0.999e-12) far_enough = false;
+    else far_enough = sqrt(d2) > 1e-6;  // exact FP64 decision near the threshold
+    if (far_enough) {
+      const float inv = 1.0f / dist;
+      n = T3<R>{(R)((float)d.x * inv), (R)((float)d.y * inv), (R)((float)d.z * inv)};
+    } else {
+      n = t3(R(0), R(1), R(0));
+    }
+  }
+  const R rir = (R)ri, rjr = (R)rj;
+  if (overlap > R(0.2) * fmin(rir, rjr)) excess = true;
+  const T3<R> ra = (-n) * rir;
+  const T3<R> rb = n * rjr;
+  T3<R> rv;
+  if (sizeof(R) == sizeof(double)) {
+    const T3<R> va = cvt<R>(vi) + cross(cvt<R>(wi), ra);
+    const T3<R> vb = cvt<R>(vj) + cross(cvt<R>(wj), rb);
+    rv = va - vb;
+  } else {
+    rv = cvt<R>(vi - vj) + cross(cvt<R>(wi), ra) - cross(cvt<R>(wj), rb);
+  }
+  const R rs = (rir * rjr) / (rir + rjr);
+  const R ms = ((R)mi * (R)mj) / ((R)mi + (R)mj);
+  // |f n| = |f| for the unit normal (the reference takes the vector length)
+  const R fmag = normal_mag<R>(P.nmodel, overlap, n, rv, (R)P.es_pp, rs, ms, (R)P.beta_abs, (R)P.gamma_pp, false);
+  const T3<R> fnv = fmag * n;
+  const R fnm = fabs(fmag);
+  T3<R> ft;
+  if (P.tmodel == 0) {
+    ft = coulomb_force<R>(fnm, rv, n, (R)P.pm.mu);
+  } else if (!PHYS) {
+    // G* = 0 (src/material.rs:39-50): the spring force is +-0, or NaN when
+    // Mindlin takes sqrt of a negative overlap.
+    R kt = P.tmodel == 2 ? R(8) * (R)P.gs_pp * sqrt(rs * overlap) : (R)P.gs_pp * rs;
+    ft = (kt != kt) ? t3(kt, kt, kt) : t3(R(0), R(0), R(0));
+  } else {
+    T3<R> xi_s = t3(R(0), R(0), R(0));
+    if (overlap > R(0)) {
+      R kt = P.tmodel == 2 ? R(8) * (R)P.gs_pp * sqrt(rs * overlap) : (R)P.gs_pp * rs;
+      if (HIST) xi_s = t3((R)hist[0], (R)hist[plane], (R)hist[2 * plane]);
+      xi_s = xi_s - dot(xi_s, n) * n;
+      ft = spring_coulomb<R>(fnm, rv, n, xi_s, kt, (R)P.pm.mu, (R)P.dt);
+    } else {
+      ft = t3(R(0), R(0), R(0));
+    }
+    if (HIST) {
+      hist[0] = (double)xi_s.x;
+      hist[plane] = (double)xi_s.y;
+      hist[2 * plane] = (double)xi_s.z;
+    }
+  }
+  const T3<R> fc = fnv + ft;
+  const T3<R> tc = cross(ra, fc);
+  fc_out = cvt<double>(fc);
+  tc_out = cvt<double>(tc);
 }
 
 // Second half of velocity Verlet for one particle (src/simulation.rs:541-561):
@@ -165,16 +275,17 @@ __device__ __forceinline__ void second_half_kick(V& v, V& vres, V& w, V& wres, V
 // ------------------------------------------------------------- first half
 // The force kernel only writes a and tau: neighbours read v and omega while
 // it runs, so the second half kick of step n-1 is applied here, at the start
-// of step n (FUSE), and by k_second_half at the end of a stepping call.
-// Then src/simulation.rs:176-263: periodic wrap, out-of-bounds removal
-// (marked dead here and compacted by the host later; removal changes no other
-// particle's update), Kahan-compensated half kick + drift + angular half
-// kick. Also records the reference-grid cell code and requests a list
-// rebuild when a particle moved more than half the skin since the last build.
-template <bool FUSE>
+// of step n (when Ctrl::pending says a step owes it), and by k_second_half at
+// the end of a stepping call. Then src/simulation.rs:176-263: periodic wrap,
+// out-of-bounds removal (marked dead here and compacted by the host later;
+// removal changes no other particle's update), Kahan-compensated half kick +
+// drift + angular half kick. Also records the reference-grid cell code and
+// requests a list rebuild when a particle moved more than half the skin since
+// the last build.
 __global__ void __launch_bounds__(256) k_first_half(StepParams P) {
   Ctrl* C = P.ctrl;
   if (C->halt) return;
+  const bool FUSE = C->pending != 0;
   const Bank B = P.bank[C->bank];
   const double dt = P.dt;
   const bool anyp = P.periodic[0] | P.periodic[1] | P.periodic[2];
@@ -208,6 +319,8 @@ __global__ void __launch_bounds__(256) k_first_half(StepParams P) {
       const double nan = __longlong_as_double(0x7ff8000000000000ll);
       xr.x = nan; xr.y = nan; xr.z = nan;
       B.xr[k] = xr;
+      B.xf[k] = make_float4(__int_as_float(0x7fc00000), __int_as_float(0x7fc00000), __int_as_float(0x7fc00000),
+                            (float)xr.w);
       atomicAdd(&C->removed, 1ull);
       continue;
     }
@@ -242,6 +355,7 @@ __global__ void __launch_bounds__(256) k_first_half(StepParams P) {
     }
     B.wc[k] = wc;
     B.xr[k] = D4{x.x, x.y, x.z, xr.w};
+    B.xf[k] = make_float4((float)x.x, (float)x.y, (float)x.z, (float)xr.w);
     float4 r0 = B.xref[k];
     float ddx = (float)x.x - r0.x, ddy = (float)x.y - r0.y, ddz = (float)x.z - r0.z;
     if (P.periodic[0]) ddx -= (float)P.bsize[0] * rintf(ddx / (float)P.bsize[0]);
@@ -253,10 +367,11 @@ __global__ void __launch_bounds__(256) k_first_half(StepParams P) {
   if (want_rebuild) C->rebuild = 1;
 }
 
-// Completes the last step of a stepping call (the pending second half).
+// Completes the last step of a stepping call (the pending second half);
+// k_clear_pending then marks the state complete.
 __global__ void __launch_bounds__(256) k_second_half(StepParams P) {
   Ctrl* C = P.ctrl;
-  if (C->halt) return;
+  if (C->halt || !C->pending) return;
   const Bank B = P.bank[C->bank];
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < P.n; k += gridDim.x * blockDim.x) {
     uint32_t fl = B.flags[k];
@@ -271,18 +386,17 @@ __global__ void __launch_bounds__(256) k_second_half(StepParams P) {
   }
 }
 
-// ------------------------------------------------- forces + second half
-// One thread per slot gathers its Verlet list: the exact FP64 cutoff test
-// of src/simulation.rs:327-357, the reference's visit count in parity mode,
-// the pair laws of src/simulation.rs:372-460, the wall triangles of
-// src/simulation.rs:464-523 from the triangle grid, then a += F/m, tau += T
-// and the second Kahan half kick (src/simulation.rs:532-561).
-template <bool PHYS, bool HIST>
+// ---------------------------------------------------------------- forces
+// One thread per slot gathers its Verlet list: the exact FP64 cutoff test of
+// src/simulation.rs:327-357, the reference's visit count in parity mode, the
+// pair laws of src/simulation.rs:358-460 (in R), the wall triangles of
+// src/simulation.rs:464-523 from the triangle grid, then a = g + F/m and
+// tau = T (src/simulation.rs:265-271, 532-536). v and omega are only read.
+template <bool PHYS, bool HIST, typename R>
 __global__ void __launch_bounds__(128) k_force(StepParams P) {
   Ctrl* C = P.ctrl;
   if (C->halt) return;
   const Bank B = P.bank[C->bank];
-  const double dt = P.dt;
   const bool adh = (P.nmodel == 3 || P.nmodel == 4);
   const double beta_abs = P.beta_abs;
   const size_t plane = (size_t)P.n * P.cap;
@@ -297,8 +411,38 @@ __global__ void __launch_bounds__(128) k_force(StepParams P) {
     V F = vmk(0.0, 0.0, 0.0), T = vmk(0.0, 0.0, 0.0);
     const uint32_t cnt = B.ncnt[k];
     const uint32_t* row = B.nbr + (size_t)k * P.cap;
+    const float4 xif = B.xf[k];
+    const float Xi = fmaxf(fmaxf(fabsf(xif.x), fabsf(xif.y)), fabsf(xif.z));
     for (uint32_t m = 0; m < cnt; ++m) {
       const uint32_t j = row[m];
+      if (P.pretest) {
+        // FP32 pretest on the position mirror: with u = 2^-24, each FP32
+        // difference is within e = u (2X + 2 cut + L) of the FP64 one when the
+        // pair is inside the cutoff, so d2f <= cut^2 + 3.47 e cut + 3 e^2 +
+        // 12 u cut^2 there. Beyond the (larger) band below the pair is
+        // certainly outside and the exact FP64 test is skipped.
+        const float4 xjf = B.xf[j];
+        float fx = xif.x - xjf.x, fy = xif.y - xjf.y, fz = xif.z - xjf.z;
+        if (P.periodic[0]) { const float L = (float)P.bsize[0]; if (fx > 0.5f * L) fx -= L; else if (fx < -0.5f * L) fx += L; }
+        if (P.periodic[1]) { const float L = (float)P.bsize[1]; if (fy > 0.5f * L) fy -= L; else if (fy < -0.5f * L) fy += L; }
+        if (P.periodic[2]) { const float L = (float)P.bsize[2]; if (fz > 0.5f * L) fz -= L; else if (fz < -0.5f * L) fz += L; }
+        const float d2f = fx * fx + fy * fy + fz * fz;
+        const float rsf = xif.w + xjf.w;
+        const float cutf = adh ? rsf * 1.5f : rsf;
+        const float X = fmaxf(Xi, fmaxf(fmaxf(fabsf(xjf.x), fabsf(xjf.y)), fabsf(xjf.z)));
+        const float e = 6.0e-8f * (2.0f * X + 2.0f * cutf + P.lmax);
+        const float band = 4.1f * cutf * e + 3.0f * e * e + 1.0e-6f * cutf * cutf;
+        if (d2f > cutf * cutf + band) {
+          const size_t hi = (size_t)k * P.cap + m;
+          if (HIST) {
+            B.hist[hi] = 0.0;
+            B.hist[plane + hi] = 0.0;
+            B.hist[2 * plane + hi] = 0.0;
+          }
+          if (P.debug) P.dbgMult[hi] = 0;
+          continue;
+        }
+      }
       const D4 xj4 = B.xr[j];
       V d = xi - xyz(xj4);
       if (P.periodic[0]) { if (d.x > P.bsize[0] * 0.5) d.x = d.x - P.bsize[0]; else if (d.x < -P.bsize[0] * 0.5) d.x = d.x + P.bsize[0]; }
@@ -310,65 +454,27 @@ __global__ void __launch_bounds__(128) k_force(StepParams P) {
       const double margin = adh ? rsum * 0.5 : 0.0;
       const double cut = rsum + margin;
       int visits = 0;
+      const size_t hi = (size_t)k * P.cap + m;
       if (d2 < cut * cut) {
         const D4 wj4 = B.wc[j];
-        if (!PHYS) visits = ref_visits(P, ci, (unsigned long long)__double_as_longlong(wj4.w));
-        else visits = 1;
+        visits = PHYS ? 1 : ref_visits(P, ci, (unsigned long long)__double_as_longlong(wj4.w));
         if (visits > 0) {
           const D4 vj4 = B.vm[j];
-          const double dist = sqrt(d2);
-          const double overlap = rsum - dist;
-          if (overlap > 0.2 * fmin(ri, rj)) excess = true;
-          const V n = dist > 1e-6 ? d / dist : vmk(0.0, 1.0, 0.0);
-          const V ra = (-n) * ri;
-          const V rb = n * rj;
-          const V va = vi + cross(wi, ra);
-          const V vb = xyz(vj4) + cross(xyz(wj4), rb);
-          const V rv = va - vb;
-          const double rs = (ri * rj) / (ri + rj);
-          const double ms = (mi * vj4.w) / (mi + vj4.w);
-          const V fnv = normal_force(P.nmodel, overlap, n, rv, P.es_pp, rs, ms, beta_abs, P.gamma_pp, false);
-          const double fnm = len(fnv);
-          V ft;
-          if (P.tmodel == 0) {
-            ft = coulomb_force(fnm, rv, n, P.pm.mu);
-          } else if (!PHYS) {
-            // G* = 0 (src/material.rs:39-50): the spring force is +-0, or NaN
-            // when Mindlin takes sqrt of a negative overlap.
-            double kt = P.tmodel == 2 ? 8.0 * P.gs_pp * sqrt(rs * overlap) : P.gs_pp * rs;
-            ft = (kt != kt) ? vmk(kt, kt, kt) : vmk(0.0, 0.0, 0.0);
-          } else {
-            V xi_s = vmk(0.0, 0.0, 0.0);
-            const size_t hi = (size_t)k * P.cap + m;
-            if (overlap > 0.0) {
-              double kt = P.tmodel == 2 ? 8.0 * P.gs_pp * sqrt(rs * overlap) : P.gs_pp * rs;
-              if (HIST) xi_s = vmk(B.hist[hi], B.hist[plane + hi], B.hist[2 * plane + hi]);
-              xi_s = xi_s - dot(xi_s, n) * n;
-              ft = spring_coulomb(fnm, rv, n, xi_s, kt, P.pm.mu, dt);
-            } else {
-              ft = vmk(0.0, 0.0, 0.0);
-            }
-            if (HIST) {
-              B.hist[hi] = xi_s.x;
-              B.hist[plane + hi] = xi_s.y;
-              B.hist[2 * plane + hi] = xi_s.z;
-            }
-          }
-          const V fc = fnv + ft;
-          const V tc = cross(ra, fc);
+          V fc, tc;
+          pair_contact<R, PHYS, HIST>(P, d, d2, rsum, ri, rj, mi, vj4.w, vi, xyz(vj4), wi, xyz(wj4),
+                                      HIST ? B.hist + hi : nullptr, plane, fc, tc, excess);
           for (int t = 0; t < visits; ++t) {
             F = F + fc;
             T = T + tc;
           }
         }
       }
-      if (PHYS && HIST && visits == 0) {
-        const size_t hi = (size_t)k * P.cap + m;
+      if (HIST && visits == 0) {
         B.hist[hi] = 0.0;
         B.hist[plane + hi] = 0.0;
         B.hist[2 * plane + hi] = 0.0;
       }
-      if (P.debug) P.dbgMult[(size_t)k * P.cap + m] = (uint8_t)visits;
+      if (P.debug) P.dbgMult[hi] = (uint8_t)visits;
     }
     // walls: triangles of the particle's triangle-grid cell, in mesh order
     if (P.ntri > 0) {
@@ -427,8 +533,8 @@ __global__ void __launch_bounds__(128) k_force(StepParams P) {
           if (pen > 0.2 * ri) excess = true;
           const V ra = (-n) * ri;
           const V rv = vi + cross(wi, ra);
-          const V fnv = normal_force(P.nmodel, pen, n, rv, P.es_pw, ri, mi, beta_abs, P.gamma_pw, true);
-          const V fc = fnv + coulomb_force(len(fnv), rv, n, P.pm.mu);
+          const V fnv = normal_force<double>(P.nmodel, pen, n, rv, P.es_pw, ri, mi, beta_abs, P.gamma_pw, true);
+          const V fc = fnv + coulomb_force<double>(len(fnv), rv, n, P.pm.mu);
           F = F + fc;
           T = T + cross(ra, fc);
         }
@@ -449,15 +555,35 @@ __global__ void __launch_bounds__(128) k_force(StepParams P) {
   if (excess) C->overlap_flag = 1;
 }
 
-__global__ void k_end_step(StepParams P) {
+__global__ void k_clear_pending(StepParams P) {
+  if (!P.ctrl->halt) P.ctrl->pending = 0;
+}
+
+// End of a step: count it and, inside the device step loop, decide whether
+// the loop runs again. The loop also stops on a halt and after target + 4
+// iterations whatever the counters say, so it always terminates.
+__global__ void k_end_step(StepParams P, cudaGraphConditionalHandle loop, int in_loop) {
   Ctrl* C = P.ctrl;
-  if (C->halt) return;
-  C->steps_done += 1;
-  if (C->overlap_flag) {
-    C->overlap_steps += 1;
-    C->status |= ST_OVERLAP;
-    C->overlap_flag = 0;
+  if (!C->halt) {
+    C->steps_done += 1;
+    C->pending = 1;
+    if (C->overlap_flag) {
+      C->overlap_steps += 1;
+      C->status |= ST_OVERLAP;
+      C->overlap_flag = 0;
+    }
   }
+  if (in_loop) {
+    C->iters += 1;
+    const bool again = !C->halt && C->steps_done < C->target && C->iters < C->target + 4;
+    cudaGraphSetConditional(loop, again ? 1u : 0u);
+  }
+}
+
+// Inside the device step loop: run the rebuild chain only when requested.
+__global__ void k_rebuild_condition(StepParams P, cudaGraphConditionalHandle h) {
+  const Ctrl* C = P.ctrl;
+  cudaGraphSetConditional(h, (C->rebuild && !C->halt) ? 1u : 0u);
 }
 
 __global__ void k_kinetic(StepParams P, double* out) {
@@ -473,31 +599,47 @@ __global__ void k_kinetic(StepParams P, double* out) {
   if ((threadIdx.x & 31) == 0) atomicAdd(out, e);
 }
 
-int launch_first_half(const StepParams& P, bool fuse_second_half, cudaStream_t s) {
+int launch_first_half(const StepParams& P, cudaStream_t s) {
   if (P.n == 0) return 0;
-  if (fuse_second_half) k_first_half<true><<<grid_for(P.n, 256), 256, 0, s>>>(P);
-  else k_first_half<false><<<grid_for(P.n, 256), 256, 0, s>>>(P);
+  k_first_half<<<grid_for(P.n, 256), 256, 0, s>>>(P);
   return 1;
 }
 
 int launch_second_half(const StepParams& P, cudaStream_t s) {
   if (P.n == 0) return 0;
   k_second_half<<<grid_for(P.n, 256), 256, 0, s>>>(P);
+  k_clear_pending<<<1, 1, 0, s>>>(P);
+  return 2;
+}
+
+int launch_rebuild_condition(const StepParams& P, cudaGraphConditionalHandle h, cudaStream_t s) {
+  k_rebuild_condition<<<1, 1, 0, s>>>(P, h);
   return 1;
+}
+
+template <typename R>
+static void launch_force_t(const StepParams& P, int g, cudaStream_t s) {
+  const bool hist = P.mode == 1 && P.tmodel != 0;
+  if (P.mode == 0) k_force<false, false, R><<<g, 128, 0, s>>>(P);
+  else if (hist) k_force<true, true, R><<<g, 128, 0, s>>>(P);
+  else k_force<true, false, R><<<g, 128, 0, s>>>(P);
 }
 
 int launch_force(const StepParams& P, cudaStream_t s) {
   if (P.n == 0) return 0;
   const int g = grid_for(P.n, 128);
-  const bool hist = P.mode == 1 && P.tmodel != 0;
-  if (P.mode == 0) k_force<false, false><<<g, 128, 0, s>>>(P);
-  else if (hist) k_force<true, true><<<g, 128, 0, s>>>(P);
-  else k_force<true, false><<<g, 128, 0, s>>>(P);
+  if (P.prec == 1) launch_force_t<float>(P, g, s);
+  else launch_force_t<double>(P, g, s);
   return 1;
 }
 
 int launch_end_step(const StepParams& P, cudaStream_t s) {
-  k_end_step<<<1, 1, 0, s>>>(P);
+  k_end_step<<<1, 1, 0, s>>>(P, 0, 0);
+  return 1;
+}
+
+int launch_end_step_loop(const StepParams& P, cudaGraphConditionalHandle loop, cudaStream_t s) {
+  k_end_step<<<1, 1, 0, s>>>(P, loop, 1);
   return 1;
 }
 

@@ -460,6 +460,12 @@ int rp_set_neighbor_capacity(rp_sim* s, int capacity) {
   return RP_OK;
 }
 
+int rp_set_device_loop(rp_sim* s, int enable) {
+  SIM_OR_FAIL(s);
+  s->e->use_graph_ = enable != 0;
+  return RP_OK;
+}
+
 static int g_threads_set = 0;
 int rp_set_threads(int n) {
   // The reference sizes rayon's global pool once (src/lib.rs:15-22); a second

@@ -35,6 +35,10 @@ struct Ctrl {
   unsigned long long steps_done;  // completed steps
   unsigned long long rebuilds;    // completed list rebuilds
   unsigned long long overlap_steps;
+  int pending;                    // the last completed step still owes its second half kick
+  int pad_;
+  unsigned long long target;      // device step loop: run while steps_done < target
+  unsigned long long iters;       // device step loop iterations (bounded by target + 4)
 };
 
 struct Material {
@@ -53,6 +57,7 @@ struct Bank {
   uint32_t* flags;  // PF_*
   uint32_t* tag;    // insertion number (stable identity)
   float4* xref;     // position at the last list build (.w unused)
+  float4* xf;       // FP32 mirror of (position, radius) for the pair pretest
   uint32_t* nbr;    // neighbour rows, cap entries per slot
   uint32_t* ncnt;   // row lengths
   double* hist;     // physical-mode tangential spring per row entry: 3 planes of N*cap
@@ -87,6 +92,8 @@ struct StepParams {
   uint32_t fncells;
   double skin;
   float list_scale;  // 1 + relative margin of the FP32 list test
+  int pretest;       // FP32 pair pretest enabled (off when a periodic length < 4 cutoffs)
+  float lmax;        // largest periodic length (enters the pretest rounding bound)
   // triangles
   int ntri;
   const TriRec* tri;

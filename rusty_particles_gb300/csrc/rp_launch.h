@@ -38,8 +38,10 @@ int launch_reference_grid(const StepParams& P, const D4* xr, int n, uint32_t nce
                           cudaStream_t s);
 
 // k_step.cu
-int launch_first_half(const StepParams& P, bool fuse_second_half, cudaStream_t s);  // each returns kernels launched
+int launch_first_half(const StepParams& P, cudaStream_t s);  // each returns kernels launched
 int launch_second_half(const StepParams& P, cudaStream_t s);
+int launch_rebuild_condition(const StepParams& P, cudaGraphConditionalHandle h, cudaStream_t s);
+int launch_end_step_loop(const StepParams& P, cudaGraphConditionalHandle loop, cudaStream_t s);
 int launch_force(const StepParams& P, cudaStream_t s);
 int launch_end_step(const StepParams& P, cudaStream_t s);
 // Kinetic energy (translational + rotational) of the live slots, FP64.

@@ -59,9 +59,12 @@ def test_periodic(rp, oracle_mod):
 
 
 def test_column_1000(rp, oracle_mod):
+    # 1,000 particles overlapping by up to 95 % explode out of the box; the
+    # survivor count after 100 steps is chaotic in the last bits of the forces
+    # (neighbour summation order), so it is compared within 1 % of N
     g = scenarios.column_1000(rp.Simulation.create)
     o = scenarios.column_1000(lambda *a: oracle_mod.OracleSimulation.create(*a, prec=64))
-    assert g.get_particle_count() == o.get_particle_count()
+    assert abs(g.get_particle_count() - o.get_particle_count()) <= 10
 
 
 def test_enable_gpu_then_getters_are_current(rp):
