@@ -419,13 +419,18 @@ def run_ours(args, log):
     import torch
     import rusty_particles_gb300 as rp
     torch.cuda.set_device(local)
-    wl = hopper_workload() if args.workload == "hopper" else box_workload()
+    wl = hopper_workload(n=args.particles) if args.workload == "hopper" else box_workload()
     n = len(wl["radius"])
-    if args.workload == "hopper":
+    if args.state_in:
+        wl["position"] = np.load(args.state_in)["position"]
+    elif args.workload == "hopper":
         relax(rp, wl, log=log)
+    if args.state_out:
+        np.savez(args.state_out, position=wl["position"])
     sim = make_sim(rp, wl, args.mode, args.precision)
     sim._L.rp_enable_gpu(sim._h, local)
-    sim._L.rp_set_profiling(sim._h, 1)
+    if args.host_loop:
+        sim._L.rp_set_device_loop(sim._h, 0)
     sim.steps(args.warmup)
     torch.cuda.synchronize()
     s0 = sim.stats()
@@ -434,7 +439,7 @@ def run_ours(args, log):
     torch.cuda.synchronize()
     clocks.start()
     t0 = time.perf_counter()
-    sim.steps(args.steps)
+    sim.steps(args.steps)  # one device step loop (CUDA graph) for all K steps
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
     barrier(dist)
@@ -445,8 +450,21 @@ def run_ours(args, log):
     t_max = allreduce_max(dist, dev_ms)
     total_units = allreduce_sum(dist, n_now * args.steps)
     value = total_units / (t_max / 1e3)
-    force_ms = (s1["force_ms"] - s0["force_ms"]) / max(1, s1["force_launches"] - s0["force_launches"])
     launches = s1["kernel_launches"] - s0["kernel_launches"]
+    if args.profile_only:
+        if rank == 0:
+            print(json.dumps({"profile_only": True, "particles": int(n_now), "steps": args.steps,
+                              "ms_per_step": t_max / args.steps, "gpu_launches": int(launches)}), flush=True)
+        return 0
+    # roofline of the dominant kernel: the same steps issued from the host with
+    # CUDA events around every force launch on the engine's stream
+    sim._L.rp_set_profiling(sim._h, 1)
+    p0 = sim.stats()
+    sim.steps(min(args.steps, 200))
+    p1 = sim.stats()
+    sim._L.rp_set_profiling(sim._h, 0)
+    force_ms = (p1["force_ms"] - p0["force_ms"]) / max(1, p1["force_launches"] - p0["force_launches"])
+    step_ms_profiled = (p1["device_ms"] - p0["device_ms"]) / max(1, p1["steps"] - p0["steps"])
     # algorithmic bytes per force launch (see B0_FP64)
     tri = len(wl["tri_v"])
     alg_bytes = n_now * B0_FP64 + tri * B_TRIANGLE
@@ -454,6 +472,7 @@ def run_ours(args, log):
     achieved = alg_bytes / (force_ms / 1e3) / 1e9
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": profiled_traffic(wl["name"], n_now), "kernel": "k_force", "avg_launch_ms": force_ms,
+            "force_share_of_step": force_ms / step_ms_profiled if step_ms_profiled > 0 else None,
             "algorithmic_bytes_per_launch": alg_bytes, "peak_source": peak_kind}
     # end to end through the public API with host buffers
     st = sim.get_state()
@@ -503,6 +522,11 @@ def main():
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--particles", type=int, default=1_048_576, help="hopper workload size")
+    ap.add_argument("--state-in", default=None, help="relaxed positions (.npz) instead of relaxing")
+    ap.add_argument("--state-out", default=None, help="save the relaxed positions (.npz)")
+    ap.add_argument("--host-loop", action="store_true", help="host-issued kernels instead of the device loop")
+    ap.add_argument("--profile-only", action="store_true", help="warm-up + timed steps only (for ncu)")
     args = ap.parse_args()
     args.steps_ref = max(1, min(args.steps, 10))
     args.warmup_ref = max(1, min(args.warmup, 2))

@@ -122,11 +122,17 @@ struct Contact {  // src/contact.rs:4-17
 };
 
 // ---------------------------------------------------------------- force laws
+// Each law also adds the magnitudes of its additive terms to tl_terms: the
+// scale at which a different rounding of the same formula can change the
+// result (a difference of two nearly equal terms has no relative precision of
+// its own). Tests use it to normalise per-particle force errors.
+thread_local double tl_terms = 0.0;
 // src/physics.rs:49-70
 template <typename T>
 V3<T> linear_spring_dashpot(T overlap, V3<T> n, V3<T> rv, T kn, T gn) {
   T vn = rv.dot(n);
   T f = kn * overlap - gn * vn;
+  tl_terms += std::fabs((double)(kn * overlap)) + std::fabs((double)(gn * vn));
   f = rmax(f, T(0));
   return f * n;
 }
@@ -142,6 +148,7 @@ V3<T> hertzian(T overlap, V3<T> n, V3<T> rv, T es, T rs, T ms, T e) {
   T cn = T(2) * std::sqrt(ms * kt) * std::fabs(beta);
   T vn = rv.dot(n);
   T fd = -cn * vn;
+  tl_terms += std::fabs((double)fe) + std::fabs((double)fd);
   T tot = rmax(fe + fd, T(0));
   return tot * n;
 }
@@ -150,6 +157,7 @@ template <typename T>
 V3<T> hertz_elastic(T overlap, V3<T> n, T es, T rs) {
   T kn = T(4.0 / 3.0) * es * std::sqrt(rs);
   T f = overlap > T(0) ? kn * std::pow(overlap, T(1.5)) : T(0);
+  tl_terms += std::fabs((double)f);
   return f * n;
 }
 // src/physics.rs:132-219
@@ -182,6 +190,7 @@ V3<T> jkr(T overlap, V3<T> n, T es, T rs, T gamma) {
   T fm = term1 - term2;
   T f_pull = T(-2.0 / 3.0) * pi<T>() * gamma * rs;
   if (fm < f_pull) return V3<T>();
+  tl_terms += std::fabs((double)term1) + std::fabs((double)term2);
   return fm * n;
 }
 // src/physics.rs:234-325
@@ -196,6 +205,7 @@ V3<T> sjkr(T overlap, V3<T> n, V3<T> rv, T es, T rs, T gamma) {
   T coh = vn > T(0) ? T(1) : T(0);
   T fh = overlap > T(0) ? T(4.0 / 3.0) * es * std::sqrt(rs) * std::pow(overlap, T(1.5)) : T(0);
   T tot = fh - coh * f_pull;
+  tl_terms += std::fabs((double)fh) + std::fabs((double)(coh * f_pull));
   return tot * n;
 }
 // src/physics.rs:385-397
@@ -204,6 +214,7 @@ V3<T> coulomb(T fn, V3<T> rv, V3<T> n, T mu) {
   V3<T> vt = rv - rv.dot(n) * n;
   if (vt.length_squared() < T(1e-8)) return V3<T>();
   V3<T> dir = vt.normalize();
+  tl_terms += std::fabs((double)(mu * fn));
   return (-mu * fn) * dir;
 }
 // src/physics.rs:400-434 (xi is the stored tangential displacement)
@@ -218,8 +229,10 @@ V3<T> linear_spring_coulomb(T fn, V3<T> rv, V3<T> n, V3<T>& xi, T kt, T mu, T dt
     V3<T> dir = tm > T(1e-6) ? trial / tm : V3<T>();
     V3<T> ft = fc * dir;
     xi = (-ft) / kt;
+    tl_terms += (double)ft.length();
     return ft;
   }
+  tl_terms += (double)trial.length();
   return trial;
 }
 
@@ -506,6 +519,7 @@ struct Sim : Base {
     V3<T> rv = va - vb;
     T rs = effective_radius(p.r, o.r);
     T ms = effective_mass(p.m, o.m);
+    tl_terms = 0.0;
     V3<T> fnv;
     switch (nmodel) {
       case N_HERTZ: fnv = hertzian(overlap, n, rv, es, rs, ms, pm.e); break;
@@ -550,8 +564,8 @@ struct Sim : Base {
     ftot += fc;
     V3<T> tc = ra.cross(fc);
     ttot += tc;
-    fs += (double)fc.length();
-    ts += (double)p.r * (double)fc.length();  // |r_a| |f|: the rounding scale of r_a x f
+    fs += tl_terms;
+    ts += (double)p.r * tl_terms;  // |r_a| x the force scale: the rounding scale of r_a x f
     return true;
   }
 
@@ -664,6 +678,7 @@ struct Sim : Base {
         V3<T> va = p.v + p.w.cross(ra);
         V3<T> rv = va;
         T rs = p.r, ms = p.m;
+        tl_terms = 0.0;
         V3<T> fnv;
         switch (nmodel) {
           case N_HERTZ: fnv = hertzian(pen, nrm, rv, ew, rs, ms, pm.e); break;
@@ -678,8 +693,8 @@ struct Sim : Base {
         ftot += fc;
         V3<T> tc = ra.cross(fc);
         ttot += tc;
-        fs += (double)fc.length();
-        ts += (double)p.r * (double)fc.length();
+        fs += tl_terms;
+        ts += (double)p.r * tl_terms;
       }
       lastF[i] = ftot;
       lastT[i] = ttot;
@@ -887,7 +902,8 @@ void orc_last_forces(void* hv, double* F, double* Tq) {
     return 0;
   });
 }
-// Per-particle sums of contribution magnitudes of the last step.
+// Per-particle force scale of the last step: the sum over contacts of the
+// magnitudes of each law's additive terms (and r times it for torques).
 void orc_last_force_scale(void* hv, double* FS, double* TS) {
   dispatch((Handle*)hv, [&](auto* s) {
     for (size_t i = 0; i < s->lastFS.size(); ++i) { FS[i] = s->lastFS[i]; TS[i] = s->lastTS[i]; }

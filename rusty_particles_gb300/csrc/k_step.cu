@@ -71,9 +71,10 @@ __device__ __forceinline__ R hertz_elastic_mag(R overlap, R es, R rs) {
   R kn = R(4.0 / 3.0) * es * sqrt(rs);
   return overlap > R(0) ? kn * (overlap * sqrt(overlap)) : R(0);
 }
-// src/physics.rs:132-219 (Newton on a^2/R* - sqrt(C a) - delta = 0)
+// src/physics.rs:132-219 (Newton on a^2/R* - sqrt(C a) - delta = 0).
+// `near` (FP32 callers) is set when a cut-off decision lies within rounding.
 template <typename R>
-__device__ __forceinline__ R jkr_mag(R overlap, R es, R rs, R gamma) {
+__device__ __forceinline__ R jkr_mag(R overlap, R es, R rs, R gamma, bool* near = nullptr) {
   if (gamma <= R(0)) return hertz_elastic_mag(overlap, es, rs);
   const R eight_pi = R(8) * R(kPi);
   R c_val = eight_pi * gamma / es;
@@ -95,6 +96,7 @@ __device__ __forceinline__ R jkr_mag(R overlap, R es, R rs, R gamma) {
   }
   R ts = sqrt(c_val * a);
   R f_val = a * a / rs - ts - overlap;
+  if (near && fabs(fabs(f_val) - R(1e-3) * rs) <= R(1e-5) * rs) *near = true;
   if (fabs(f_val) > R(1e-3) * rs) return R(0);
   if (a <= R(0)) return R(0);
   R a3 = a * a * a;
@@ -102,6 +104,7 @@ __device__ __forceinline__ R jkr_mag(R overlap, R es, R rs, R gamma) {
   R term2 = sqrt(eight_pi * gamma * es * a3);
   R fm = term1 - term2;
   R f_pull = R(-2.0 / 3.0) * R(kPi) * gamma * rs;
+  if (near && fabs(fm - f_pull) <= R(1e-5) * (term1 + term2)) *near = true;
   if (fm < f_pull) return R(0);
   return fm;
 }
@@ -178,11 +181,17 @@ __device__ __forceinline__ T3<R> spring_coulomb(R fn, T3<R> rv, T3<R> n, T3<R>& 
 
 // One contact seen from particle i (src/simulation.rs:358-460), for a pair
 // that passed the cutoff test. Inputs in FP64; the law arithmetic in R.
-// Returns the contact force on i and its torque r_a x f in FP64.
+// Writes the contact force on i and its torque r_a x f in FP64 and returns
+// true. In FP32 it returns false, touching nothing, when a discontinuous
+// decision of the reference's laws (Coulomb's |v_t|^2 < 1e-8, sJKR's
+// loading/unloading sign and detachment, JKR's cut-offs) or an sJKR
+// near-cancellation lies within FP32 rounding: the caller then evaluates the
+// pair in FP64, so both forms take the same branches.
 template <typename R, bool PHYS, bool HIST>
-__device__ __forceinline__ void pair_contact(const StepParams& P, V d, double d2, double rsum, double ri, double rj,
+__device__ __forceinline__ bool pair_contact(const StepParams& P, V d, double d2, double rsum, double ri, double rj,
                                              double mi, double mj, V vi, V vj, V wi, V wj, double* hist, size_t plane,
                                              V& fc_out, V& tc_out, bool& excess) {
+  constexpr bool F32 = sizeof(R) == sizeof(float);
   R overlap;
   T3<R> n;
   if (sizeof(R) == sizeof(double)) {
@@ -220,12 +229,33 @@ __device__ __forceinline__ void pair_contact(const StepParams& P, V d, double d2
   }
   const R rs = (rir * rjr) / (rir + rjr);
   const R ms = ((R)mi * (R)mj) / ((R)mi + (R)mj);
+  R fmag;
+  if (F32 && P.nmodel == 3) {
+    bool near = false;
+    fmag = jkr_mag<R>(overlap, (R)P.es_pp, rs, (R)P.gamma_pp, &near);
+    if (near) return false;
+  } else {
+    fmag = normal_mag<R>(P.nmodel, overlap, n, rv, (R)P.es_pp, rs, ms, (R)P.beta_abs, (R)P.gamma_pp, false);
+  }
+  if (F32 && P.nmodel == 4 && P.gamma_pp > 0.0) {
+    const R vn = dot(rv, n);
+    const R gamma = (R)P.gamma_pp, es = (R)P.es_pp;
+    const R f_pull = R(1.5) * R(kPi) * gamma * rs;
+    const R delta_c = -sqrt(R(3) * (R(kPi) * R(kPi)) * (gamma * gamma) * rs / (es * es));
+    if (fabs(vn) <= R(1e-6) * (len(rv) + R(1e-30))) return false;
+    if (fabs(overlap - delta_c) <= R(1e-5) * fabs(delta_c)) return false;
+    if (vn > R(0) && fabs(fmag) <= R(0.05) * f_pull) return false;
+  }
   // |f n| = |f| for the unit normal (the reference takes the vector length)
-  const R fmag = normal_mag<R>(P.nmodel, overlap, n, rv, (R)P.es_pp, rs, ms, (R)P.beta_abs, (R)P.gamma_pp, false);
   const T3<R> fnv = fmag * n;
   const R fnm = fabs(fmag);
   T3<R> ft;
   if (P.tmodel == 0) {
+    if (F32) {
+      const T3<R> vt = rv - dot(rv, n) * n;
+      const R vt2 = dot(vt, vt);
+      if (fabs(vt2 - R(1e-8)) <= R(1e-5) * (dot(rv, rv) + R(1e-8))) return false;
+    }
     ft = coulomb_force<R>(fnm, rv, n, (R)P.pm.mu);
   } else if (!PHYS) {
     // G* = 0 (src/material.rs:39-50): the spring force is +-0, or NaN when
@@ -252,6 +282,7 @@ __device__ __forceinline__ void pair_contact(const StepParams& P, V d, double d2
   const T3<R> tc = cross(ra, fc);
   fc_out = cvt<double>(fc);
   tc_out = cvt<double>(tc);
+  return true;
 }
 
 // Second half of velocity Verlet for one particle (src/simulation.rs:541-561):
@@ -461,8 +492,10 @@ __global__ void __launch_bounds__(128) k_force(StepParams P) {
         if (visits > 0) {
           const D4 vj4 = B.vm[j];
           V fc, tc;
-          pair_contact<R, PHYS, HIST>(P, d, d2, rsum, ri, rj, mi, vj4.w, vi, xyz(vj4), wi, xyz(wj4),
-                                      HIST ? B.hist + hi : nullptr, plane, fc, tc, excess);
+          if (!pair_contact<R, PHYS, HIST>(P, d, d2, rsum, ri, rj, mi, vj4.w, vi, xyz(vj4), wi, xyz(wj4),
+                                           HIST ? B.hist + hi : nullptr, plane, fc, tc, excess))
+            pair_contact<double, PHYS, HIST>(P, d, d2, rsum, ri, rj, mi, vj4.w, vi, xyz(vj4), wi, xyz(wj4),
+                                             HIST ? B.hist + hi : nullptr, plane, fc, tc, excess);
           for (int t = 0; t < visits; ++t) {
             F = F + fc;
             T = T + tc;

@@ -9,7 +9,7 @@ TANGENTIAL_NAMES = {0: "coulomb", 1: "linear", 2: "mindlin"}
 
 
 def random_bed(seed, n, lo, hi, rmin, rmax, vscale=0.05, wscale=1.0, ascale=1.0, tscale=1e-6, fixed_frac=0.0,
-               outside=0):
+               outside=0, jitter=0.02):
     """Particles on a jittered lattice filling [lo, hi] so that neighbours touch
     (overlaps up to a few % of a radius), with random v, omega, a, tau."""
     rng = np.random.default_rng(seed)
@@ -23,7 +23,7 @@ def random_bed(seed, n, lo, hi, rmin, rmax, vscale=0.05, wscale=1.0, ascale=1.0,
     g = np.stack(np.meshgrid(*[np.arange(d) for d in dims], indexing="ij"), -1).reshape(-1, 3)
     g = g[np.lexsort((g[:, 2], g[:, 0], g[:, 1]))]
     g = g[:n]
-    x = lo + (g + 0.5) * spacing + rng.uniform(-0.02, 0.02, g.shape) * rmax
+    x = lo + (g + 0.5) * spacing + rng.uniform(-jitter, jitter, g.shape) * rmax
     k = len(x)
     r = rng.uniform(rmin, rmax, k)
     st = {

@@ -168,13 +168,14 @@ def test_mixed_precision_one_step(rp, oracle_mod, normal):
 
 
 def test_many_steps_stay_close(rp, oracle_mod):
-    # Gently touching bed (overlaps <= 2 % of a radius): 200 steps stay within
-    # rounding of the oracle. (Beds overlapping by ~35 % are chaotic: the
-    # 1e-16 summation-order difference grows ~10x every 3 steps there, so
-    # trajectories are compared statistically below instead.)
+    # Hertz with the reference's Mindlin (zero tangential force) on a touching
+    # bed: 200 steps stay within rounding of the oracle. With Coulomb friction
+    # a dense bed chatters (dF_t/dv_t ~ mu|F_n|/|v_t| amplifies a 1e-16
+    # difference ~10x every 3 steps), so that case is compared statistically
+    # in test_settling_bed_statistics.
     lo, hi = (-0.2, -0.2, -0.2), (0.2, 0.2, 0.2)
-    st = pu.random_bed(41, 1000, lo, hi, 0.0098, 0.01, vscale=0.01, ascale=0.0)
-    o, g = one_step(rp, oracle_mod, st, 1, 0, lo, hi, dt=1e-5)
+    st = pu.random_bed(41, 1000, lo, hi, 0.0099, 0.0101, vscale=0.01, ascale=0.0, jitter=0.002)
+    o, g = one_step(rp, oracle_mod, st, 1, 2, lo, hi, dt=1e-5)
     o.steps(199)
     g.steps(199)
     so, sg = o.state(), g.get_state()
@@ -201,18 +202,25 @@ def test_settling_bed_statistics(rp, oracle_mod):
     v = np.array([np.concatenate(t) for t in tris], np.float32).astype(np.float64)
     nrm = np.array([np.cross(t[1] - t[0], t[2] - t[0]) / np.linalg.norm(np.cross(t[1] - t[0], t[2] - t[0]))
                     for t in tris], np.float32).astype(np.float64)
-    st = pu.random_bed(61, 1500, (-0.1, -0.1, -0.1), (0.1, 0.3, 0.1), 0.006, 0.008, vscale=0.1, ascale=0.0)
-    o, g = one_step(rp, oracle_mod, st, 1, 0, lo, hi, dt=5e-5, tris=(v, nrm), cell=0.05)
-    o.steps(2999)
-    g.steps(2999)
-    so = o.state()
-    sgs = g.get_state()
-    sg = {"x": sgs["position"], "v": sgs["velocity"], "w": sgs["angular_velocity"], "r": sgs["radius"],
-          "m": sgs["mass"]}
-    n = len(so["r"])
+    st = pu.random_bed(61, 6000, (-0.1, -0.1, -0.1), (0.1, 0.3, 0.1), 0.004, 0.005, vscale=0.1, ascale=0.0)
+    o, g = one_step(rp, oracle_mod, st, 1, 0, lo, hi, dt=5e-5, tris=(v, nrm), cell=0.012)
+    o.steps(1999)
+    g.steps(1999)
+    kos, kgs = [], []
+    for _ in range(10):  # kinetic energy averaged over the last 1,000 steps
+        o.steps(100)
+        g.steps(100)
+        so = o.state()
+        sgs = g.get_state()
+        sg = {"x": sgs["position"], "v": sgs["velocity"], "w": sgs["angular_velocity"], "r": sgs["radius"],
+              "m": sgs["mass"]}
+        n = len(so["r"])
+        kos.append(_bed_statistics(so, {}, n, 0.04, -0.1)[0])
+        kgs.append(_bed_statistics(sg, {}, n, 0.04, -0.1)[0])
     assert g.get_particle_count() == n
-    ko, zo, po = _bed_statistics(so, pu.pair_counter_oracle(o), n, 0.04, -0.1)
-    kg, zg, pg = _bed_statistics(sg, pu.pair_counter_gpu(g), n, 0.04, -0.1)
+    _, zo, po = _bed_statistics(so, pu.pair_counter_oracle(o), n, 0.04, -0.1)
+    _, zg, pg = _bed_statistics(sg, pu.pair_counter_gpu(g), n, 0.04, -0.1)
+    ko, kg = float(np.mean(kos)), float(np.mean(kgs))
     assert abs(kg - ko) <= 0.005 * ko + 1e-12, (kg, ko)
     assert abs(zg - zo) <= 0.005 * zo, (zg, zo)
     assert abs(pg - po) <= 0.005 * po, (pg, po)
