@@ -206,8 +206,8 @@ def test_settling_bed_statistics(rp, oracle_mod):
     o, g = one_step(rp, oracle_mod, st, 1, 0, lo, hi, dt=5e-5, tris=(v, nrm), cell=0.012)
     o.steps(1999)
     g.steps(1999)
-    kos, kgs = [], []
-    for _ in range(10):  # kinetic energy averaged over the last 1,000 steps
+    so_stats, sg_stats = [], []
+    for _ in range(10):  # statistics averaged over the last 1,000 steps
         o.steps(100)
         g.steps(100)
         so = o.state()
@@ -215,12 +215,11 @@ def test_settling_bed_statistics(rp, oracle_mod):
         sg = {"x": sgs["position"], "v": sgs["velocity"], "w": sgs["angular_velocity"], "r": sgs["radius"],
               "m": sgs["mass"]}
         n = len(so["r"])
-        kos.append(_bed_statistics(so, {}, n, 0.04, -0.1)[0])
-        kgs.append(_bed_statistics(sg, {}, n, 0.04, -0.1)[0])
+        so_stats.append(_bed_statistics(so, pu.pair_counter_oracle(o), n, 0.04, -0.1))
+        sg_stats.append(_bed_statistics(sg, pu.pair_counter_gpu(g), n, 0.04, -0.1))
     assert g.get_particle_count() == n
-    _, zo, po = _bed_statistics(so, pu.pair_counter_oracle(o), n, 0.04, -0.1)
-    _, zg, pg = _bed_statistics(sg, pu.pair_counter_gpu(g), n, 0.04, -0.1)
-    ko, kg = float(np.mean(kos)), float(np.mean(kgs))
+    ko, zo, po = np.mean(so_stats, axis=0)
+    kg, zg, pg = np.mean(sg_stats, axis=0)
     assert abs(kg - ko) <= 0.005 * ko + 1e-12, (kg, ko)
     assert abs(zg - zo) <= 0.005 * zo, (zg, zo)
     assert abs(pg - po) <= 0.005 * po, (pg, po)
