@@ -193,6 +193,25 @@ int rp_debug_contact_pairs(rp_sim* sim, int64_t* pi, int64_t* pj, int32_t* visit
 int rp_debug_reference_grid(rp_sim* sim, double h, int64_t* cell_of, int64_t* order, size_t* n_order,
                             int32_t dims[3]);
 
+/* --- allocation-free cell sort (no counterpart in the reference)
+ * For callers that cannot call cudaMalloc: code issuing work inside a CUDA
+ * stream capture, engines whose pool allocator owns all device memory, and
+ * real-time loops that cannot afford cudaMalloc's device synchronisation.
+ * Same result as rp_debug_reference_grid's hash + stable radix sort, on
+ * caller-owned DEVICE buffers: positions (3n doubles), origin/cell_size/dims
+ * of the grid (the reference's formula, src/grid.rs:30-40); writes
+ * cell_of[i] (linear cell, or 0xFFFFFFFF outside the grid) and order[] (all n
+ * particle indices sorted by cell, stable in index order, outside ones last),
+ * on `stream` (a cudaStream_t; NULL = legacy default stream), asynchronously.
+ * Its temporaries live in one static device array sized for at most 262,144
+ * particles (larger n -> RP_E_INVALID_ARG); it calls no cudaMalloc/cudaFree.
+ * The array is shared by every call: calls that overlap on the GPU race and
+ * must be serialised by the caller. The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress); make that first call before
+ * any stream capture. */
+int rp_cell_sort_noalloc(const double* positions, size_t n, const double origin[3], double cell_size,
+                         const int32_t dims[3], uint32_t* cell_of, uint32_t* order, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -110,6 +110,8 @@ SIGNATURES = {
                                               ctypes.POINTER(ctypes.c_size_t)]),
     "rp_debug_reference_grid": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, _i64p, _i64p,
                                                ctypes.POINTER(ctypes.c_size_t), _i32p]),
+    "rp_cell_sort_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_size_t, _dp, ctypes.c_double, _i32p,
+                                            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
 }
 
 _lib = None
