@@ -165,6 +165,10 @@ int rp_set_neighbor_capacity(rp_sim* sim, int capacity); /* initial list slots p
  * runs all steps and rebuilds lists only when needed; 0: the host issues the
  * kernels step by step in chunks. */
 int rp_set_device_loop(rp_sim* sim, int enable);
+/* Force evaluation: 0 (default) contact-parallel (filter per particle, one
+ * thread per contact pair, per-particle sum in list order); 1 one thread per
+ * particle over its whole list. Same results within rounding. */
+int rp_set_force_path(rp_sim* sim, int path);
 int rp_set_threads(int n);                               /* set_num_threads (src/lib.rs:15-22) */
 
 /* --- metrics and errors */

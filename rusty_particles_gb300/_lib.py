@@ -99,6 +99,7 @@ SIGNATURES = {
     "rp_set_skin": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
     "rp_set_neighbor_capacity": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "rp_set_device_loop": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "rp_set_force_path": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "rp_set_threads": (ctypes.c_int, [ctypes.c_int]),
     "rp_get_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(RpStats)]),
     "rp_set_profiling": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),

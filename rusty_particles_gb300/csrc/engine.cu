@@ -100,6 +100,8 @@ void Engine::free_device() {
   dfree(rb_.ka); dfree(rb_.va); dfree(rb_.kb); dfree(rb_.vb); dfree(rb_.hist); dfree(rb_.part);
   dfree(rb_.cstart); dfree(rb_.cend); dfree(kraw_);
   dfree(dbgF_); dfree(dbgT_); dfree(dbgMult_); dfree(ke_);
+  dfree(crec_); dfree(clist_); dfree(cres_); dfree(ccnt_); dfree(ncomp_); dfree(coff_); dfree(poff_);
+  dfree(ctot_); dfree(cpart_);
   dfree(tri_d_); dfree(tstart_d_); dfree(titems_d_);
   dfree(ctrl_);
   if (ctrl_h_) cudaFreeHost(ctrl_h_);
@@ -221,6 +223,8 @@ int Engine::alloc_slots(size_t n) {
   TRY(dalloc(&rb_.hist, hn));
   TRY(dalloc(&rb_.part, scan_parts_needed(std::max<uint32_t>(hn, (uint32_t)na)) + 16));
   TRY(dalloc(&dbgF_, 3 * na)); TRY(dalloc(&dbgT_, 3 * na));
+  TRY(dalloc(&ccnt_, na)); TRY(dalloc(&ncomp_, na)); TRY(dalloc(&coff_, na)); TRY(dalloc(&poff_, na));
+  TRY(dalloc(&ctot_, 2)); TRY(dalloc(&cpart_, scan_parts_needed((uint32_t)na) + 16));
   n_alloc_ = na;
   // lists must be re-allocated for the new slot count
   for (int b = 0; b < 2; ++b) {
@@ -268,9 +272,29 @@ int Engine::alloc_lists(int cap, bool keep_current) {
   } else {
     dfree(dbgMult_);
   }
+  TRY(dalloc(&crec_, na * (size_t)cap));
+  TRY(dalloc(&clist_, na * (size_t)cap));
+  TRY(dalloc(&cres_, 6 * na * (size_t)cap));
   cap_ = cap;
   graph_dirty_ = true;
+  refresh_list_ptrs();
   return RP_OK;
+}
+
+void Engine::refresh_list_ptrs() {
+  P_.cap = cap_;
+  P_.bank[0] = bank_[0];
+  P_.bank[1] = bank_[1];
+  P_.dbgMult = dbgMult_;
+  P_.crec = crec_;
+  P_.clist = clist_;
+  P_.cres = cres_;
+  P_.ccnt = ccnt_;
+  P_.ncomp = ncomp_;
+  P_.coff = coff_;
+  P_.poff = poff_;
+  P_.ctot = ctot_;
+  P_.cpart = cpart_;
 }
 
 // ------------------------------------------------------------ parameters
@@ -366,10 +390,9 @@ int Engine::build_params() {
   TRY(build_triangle_grid(rmax));
   P.dbgF = dbgF_;
   P.dbgT = dbgT_;
-  P.dbgMult = dbgMult_;
   P.ctrl = ctrl_;
-  P.bank[0] = bank_[0];
-  P.bank[1] = bank_[1];
+  P.force_path = force_path;
+  refresh_list_ptrs();
   return RP_OK;
 }
 
@@ -622,10 +645,6 @@ int Engine::recover_halt() {
   while (ctrl_h_->halt) {
     int newcap = std::max<int>(cap_ + 8, (int)(ctrl_h_->max_count * 5 / 4 + 8));
     TRY(alloc_lists(newcap, true));
-    P_.cap = cap_;
-    P_.bank[0] = bank_[0];
-    P_.bank[1] = bank_[1];
-    P_.dbgMult = dbgMult_;
     graph_dirty_ = true;
     tot_.status |= ST_NLIST_GROW;
     int zero = 0;

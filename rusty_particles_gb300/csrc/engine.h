@@ -43,6 +43,7 @@ class Engine {
   double skin_user = -1.0;
   int debug = 0;
   int profiling = 0;
+  int force_path = 0;  // 0 contact-parallel, 1 one thread per particle
 
   int add_particle(const double x[3], double r, double m, int fixed);
   int add_triangles(size_t n, const float* v, const float* nrm);
@@ -107,6 +108,12 @@ class Engine {
   double* dbgF_ = nullptr;
   double* dbgT_ = nullptr;
   uint8_t* dbgMult_ = nullptr;
+  // contact-parallel force buffers
+  CRec* crec_ = nullptr;
+  uint32_t *ccnt_ = nullptr, *ncomp_ = nullptr, *coff_ = nullptr, *poff_ = nullptr, *clist_ = nullptr;
+  uint32_t *ctot_ = nullptr, *cpart_ = nullptr;
+  double* cres_ = nullptr;
+  void refresh_list_ptrs();
   double* ke_ = nullptr;
   TriRec* tri_d_ = nullptr;
   uint32_t *tstart_d_ = nullptr, *titems_d_ = nullptr;

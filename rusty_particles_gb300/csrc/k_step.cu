@@ -190,7 +190,7 @@ __device__ __forceinline__ T3<R> spring_coulomb(R fn, T3<R> rv, T3<R> n, T3<R>& 
 template <typename R, bool PHYS, bool HIST>
 __device__ __forceinline__ bool pair_contact(const StepParams& P, V d, double d2, double rsum, double ri, double rj,
                                              double mi, double mj, V vi, V vj, V wi, V wj, double* hist, size_t plane,
-                                             V& fc_out, V& tc_out, bool& excess) {
+                                             V& fc_out, V& tc_out, V& n_out, bool& excess) {
   constexpr bool F32 = sizeof(R) == sizeof(float);
   R overlap;
   T3<R> n;
@@ -282,6 +282,7 @@ __device__ __forceinline__ bool pair_contact(const StepParams& P, V d, double d2
   const T3<R> tc = cross(ra, fc);
   fc_out = cvt<double>(fc);
   tc_out = cvt<double>(tc);
+  n_out = cvt<double>(n);
   return true;
 }
 
@@ -417,6 +418,75 @@ __global__ void __launch_bounds__(256) k_second_half(StepParams P) {
   }
 }
 
+// Wall contacts of one particle (src/simulation.rs:464-523): the triangles
+// listed in the triangle-grid cell of its centre, in mesh order.
+__device__ __forceinline__ void wall_forces(const StepParams& P, V xi, V vi, V wi, double ri, double mi,
+                                            double beta_abs, V& F, V& T, bool& excess) {
+  if (P.ntri > 0) {
+    const double q0 = floor((xi.x - P.tmin[0]) / P.tcell);
+    const double q1 = floor((xi.y - P.tmin[1]) / P.tcell);
+    const double q2 = floor((xi.z - P.tmin[2]) / P.tcell);
+    if (q0 >= 0.0 && q1 >= 0.0 && q2 >= 0.0 && q0 < (double)P.tdims[0] && q1 < (double)P.tdims[1] &&
+        q2 < (double)P.tdims[2]) {
+      const uint32_t cell = (uint32_t)q0 + (uint32_t)P.tdims[0] * ((uint32_t)q1 + (uint32_t)P.tdims[1] * (uint32_t)q2);
+      const uint32_t s = P.tstart[cell], e = P.tstart[cell + 1];
+      for (uint32_t t = s; t < e; ++t) {
+        const TriRec& tr = P.tri[P.titems[t]];
+        // closest point, src/mesh.rs:45-117 (same regions and clamps)
+        const V v0 = vmk(tr.v0[0] - xi.x, tr.v0[1] - xi.y, tr.v0[2] - xi.z);
+        const V e0 = vmk(tr.e0[0], tr.e0[1], tr.e0[2]), e1 = vmk(tr.e1[0], tr.e1[1], tr.e1[2]);
+        const double a = tr.a, b = tr.b, c = tr.c, det = tr.det;
+        const double dd = dot(e0, v0), ee = dot(e1, v0);
+        const double s0 = b * ee - c * dd, t0 = b * dd - a * ee;
+        double sc = s0, tc = t0;
+        if (s0 + t0 < det) {
+          if (s0 < 0.0) {
+            if (t0 < 0.0) {
+              if (dd < 0.0) { sc = fmin(fmax(-dd, 0.0), a); tc = 0.0; }
+              else { sc = 0.0; tc = fmin(fmax(-ee, 0.0), c); }
+            } else { sc = 0.0; tc = fmin(fmax(-ee, 0.0), c); }
+          } else if (t0 < 0.0) {
+            sc = fmin(fmax(-dd, 0.0), a); tc = 0.0;
+          } else {
+            const double inv = 1.0 / det;
+            sc = sc * inv; tc = tc * inv;
+          }
+        } else {
+          if (s0 < 0.0) {
+            const double tmp0 = b + dd, tmp1 = c + ee;
+            if (tmp1 > tmp0) {
+              const double numer = tmp1 - tmp0;
+              sc = numer / tr.denom; sc = sc < 0.0 ? 0.0 : (sc > 1.0 ? 1.0 : sc); tc = 1.0 - sc;
+            } else { tc = fmin(fmax(-ee, 0.0), c); sc = 0.0; }
+          } else if (t0 < 0.0) {
+            if (a + dd > b + ee) {
+              const double numer = c + ee - b - dd;
+              sc = numer / tr.denom; sc = sc < 0.0 ? 0.0 : (sc > 1.0 ? 1.0 : sc); tc = 1.0 - sc;
+            } else { sc = fmin(fmax(-ee, 0.0), c); tc = 0.0; }
+          } else {
+            const double numer = c + ee - b - dd;
+            sc = numer / tr.denom; sc = sc < 0.0 ? 0.0 : (sc > 1.0 ? 1.0 : sc); tc = 1.0 - sc;
+          }
+        }
+        const V cp = vmk(tr.v0[0], tr.v0[1], tr.v0[2]) + sc * e0 + tc * e1;
+        const V dv = xi - cp;
+        const double dsq = dot(dv, dv);
+        if (!(dsq < ri * ri)) continue;
+        const double dist = sqrt(dsq);
+        const double pen = ri - dist;
+        const V n = dist > 1e-6 ? dv / dist : vmk(tr.n[0], tr.n[1], tr.n[2]);
+        if (pen > 0.2 * ri) excess = true;
+        const V ra = (-n) * ri;
+        const V rv = vi + cross(wi, ra);
+        const V fnv = normal_force<double>(P.nmodel, pen, n, rv, P.es_pw, ri, mi, beta_abs, P.gamma_pw, true);
+        const V fc = fnv + coulomb_force<double>(len(fnv), rv, n, P.pm.mu);
+        F = F + fc;
+        T = T + cross(ra, fc);
+      }
+    }
+  }
+}
+
 // ---------------------------------------------------------------- forces
 // One thread per slot gathers its Verlet list: the exact FP64 cutoff test of
 // src/simulation.rs:327-357, the reference's visit count in parity mode, the
@@ -491,11 +561,11 @@ __global__ void __launch_bounds__(128) k_force(StepParams P) {
         visits = PHYS ? 1 : ref_visits(P, ci, (unsigned long long)__double_as_longlong(wj4.w));
         if (visits > 0) {
           const D4 vj4 = B.vm[j];
-          V fc, tc;
+          V fc, tc, nrm;
           if (!pair_contact<R, PHYS, HIST>(P, d, d2, rsum, ri, rj, mi, vj4.w, vi, xyz(vj4), wi, xyz(wj4),
-                                           HIST ? B.hist + hi : nullptr, plane, fc, tc, excess))
+                                           HIST ? B.hist + hi : nullptr, plane, fc, tc, nrm, excess))
             pair_contact<double, PHYS, HIST>(P, d, d2, rsum, ri, rj, mi, vj4.w, vi, xyz(vj4), wi, xyz(wj4),
-                                             HIST ? B.hist + hi : nullptr, plane, fc, tc, excess);
+                                             HIST ? B.hist + hi : nullptr, plane, fc, tc, nrm, excess);
           for (int t = 0; t < visits; ++t) {
             F = F + fc;
             T = T + tc;
@@ -509,70 +579,7 @@ __global__ void __launch_bounds__(128) k_force(StepParams P) {
       }
       if (P.debug) P.dbgMult[hi] = (uint8_t)visits;
     }
-    // walls: triangles of the particle's triangle-grid cell, in mesh order
-    if (P.ntri > 0) {
-      const double q0 = floor((xi.x - P.tmin[0]) / P.tcell);
-      const double q1 = floor((xi.y - P.tmin[1]) / P.tcell);
-      const double q2 = floor((xi.z - P.tmin[2]) / P.tcell);
-      if (q0 >= 0.0 && q1 >= 0.0 && q2 >= 0.0 && q0 < (double)P.tdims[0] && q1 < (double)P.tdims[1] &&
-          q2 < (double)P.tdims[2]) {
-        const uint32_t cell = (uint32_t)q0 + (uint32_t)P.tdims[0] * ((uint32_t)q1 + (uint32_t)P.tdims[1] * (uint32_t)q2);
-        const uint32_t s = P.tstart[cell], e = P.tstart[cell + 1];
-        for (uint32_t t = s; t < e; ++t) {
-          const TriRec& tr = P.tri[P.titems[t]];
-          // closest point, src/mesh.rs:45-117 (same regions and clamps)
-          const V v0 = vmk(tr.v0[0] - xi.x, tr.v0[1] - xi.y, tr.v0[2] - xi.z);
-          const V e0 = vmk(tr.e0[0], tr.e0[1], tr.e0[2]), e1 = vmk(tr.e1[0], tr.e1[1], tr.e1[2]);
-          const double a = tr.a, b = tr.b, c = tr.c, det = tr.det;
-          const double dd = dot(e0, v0), ee = dot(e1, v0);
-          const double s0 = b * ee - c * dd, t0 = b * dd - a * ee;
-          double sc = s0, tc = t0;
-          if (s0 + t0 < det) {
-            if (s0 < 0.0) {
-              if (t0 < 0.0) {
-                if (dd < 0.0) { sc = fmin(fmax(-dd, 0.0), a); tc = 0.0; }
-                else { sc = 0.0; tc = fmin(fmax(-ee, 0.0), c); }
-              } else { sc = 0.0; tc = fmin(fmax(-ee, 0.0), c); }
-            } else if (t0 < 0.0) {
-              sc = fmin(fmax(-dd, 0.0), a); tc = 0.0;
-            } else {
-              const double inv = 1.0 / det;
-              sc = sc * inv; tc = tc * inv;
-            }
-          } else {
-            if (s0 < 0.0) {
-              const double tmp0 = b + dd, tmp1 = c + ee;
-              if (tmp1 > tmp0) {
-                const double numer = tmp1 - tmp0;
-                sc = numer / tr.denom; sc = sc < 0.0 ? 0.0 : (sc > 1.0 ? 1.0 : sc); tc = 1.0 - sc;
-              } else { tc = fmin(fmax(-ee, 0.0), c); sc = 0.0; }
-            } else if (t0 < 0.0) {
-              if (a + dd > b + ee) {
-                const double numer = c + ee - b - dd;
-                sc = numer / tr.denom; sc = sc < 0.0 ? 0.0 : (sc > 1.0 ? 1.0 : sc); tc = 1.0 - sc;
-              } else { sc = fmin(fmax(-ee, 0.0), c); tc = 0.0; }
-            } else {
-              const double numer = c + ee - b - dd;
-              sc = numer / tr.denom; sc = sc < 0.0 ? 0.0 : (sc > 1.0 ? 1.0 : sc); tc = 1.0 - sc;
-            }
-          }
-          const V cp = vmk(tr.v0[0], tr.v0[1], tr.v0[2]) + sc * e0 + tc * e1;
-          const V dv = xi - cp;
-          const double dsq = dot(dv, dv);
-          if (!(dsq < ri * ri)) continue;
-          const double dist = sqrt(dsq);
-          const double pen = ri - dist;
-          const V n = dist > 1e-6 ? dv / dist : vmk(tr.n[0], tr.n[1], tr.n[2]);
-          if (pen > 0.2 * ri) excess = true;
-          const V ra = (-n) * ri;
-          const V rv = vi + cross(wi, ra);
-          const V fnv = normal_force<double>(P.nmodel, pen, n, rv, P.es_pw, ri, mi, beta_abs, P.gamma_pw, true);
-          const V fc = fnv + coulomb_force<double>(len(fnv), rv, n, P.pm.mu);
-          F = F + fc;
-          T = T + cross(ra, fc);
-        }
-      }
-    }
+    wall_forces(P, xi, vi, wi, ri, mi, beta_abs, F, T, excess);
     if (P.debug) {
       P.dbgF[3 * (size_t)k] = F.x; P.dbgF[3 * (size_t)k + 1] = F.y; P.dbgF[3 * (size_t)k + 2] = F.z;
       P.dbgT[3 * (size_t)k] = T.x; P.dbgT[3 * (size_t)k + 1] = T.y; P.dbgT[3 * (size_t)k + 2] = T.z;
@@ -580,6 +587,207 @@ __global__ void __launch_bounds__(128) k_force(StepParams P) {
     if (!isfinite(F.x + F.y + F.z + T.x + T.y + T.z)) atomicOr(&C->status, (unsigned)ST_NAN);
     // apply (src/simulation.rs:532-536); the second half kick of this step
     // runs in the next k_first_half or in k_second_half
+    const V a = vmk(P.gravity[0], P.gravity[1], P.gravity[2]) + F / mi;
+    const V tau = vmk(0.0, 0.0, 0.0) + T;
+    B.acc[k] = D4{a.x, a.y, a.z, 0.0};
+    B.tq[k] = D4{tau.x, tau.y, tau.z, 0.0};
+  }
+  if (excess) C->overlap_flag = 1;
+}
+
+// ------------------------------------------------- contact-parallel forces
+// One thread per particle leaves every lane idle while a neighbour of another
+// lane is in contact (measured: ~9 of 32 lanes active, FP64 pipe saturated).
+// Here the per-particle pass only filters (FP32 pretest, exact FP64 cutoff,
+// visit counts); the pair laws run one thread per pair, each pair once, and a
+// last pass sums every particle's contact results in list order.
+
+// FP32 pretest on the position mirror: with u = 2^-24, each FP32 difference
+// is within e = u (2X + 2 cut + L) of the FP64 one when the pair is inside the
+// cutoff, so d2f <= cut^2 + 3.47 e cut + 3 e^2 + 12 u cut^2 there; beyond the
+// larger band below the pair is certainly outside the exact FP64 test.
+__device__ __forceinline__ bool pretest_far(const StepParams& P, float4 xif, float Xi, float4 xjf, bool adh) {
+  float fx = xif.x - xjf.x, fy = xif.y - xjf.y, fz = xif.z - xjf.z;
+  if (P.periodic[0]) { const float L = (float)P.bsize[0]; if (fx > 0.5f * L) fx -= L; else if (fx < -0.5f * L) fx += L; }
+  if (P.periodic[1]) { const float L = (float)P.bsize[1]; if (fy > 0.5f * L) fy -= L; else if (fy < -0.5f * L) fy += L; }
+  if (P.periodic[2]) { const float L = (float)P.bsize[2]; if (fz > 0.5f * L) fz -= L; else if (fz < -0.5f * L) fz += L; }
+  const float d2f = fx * fx + fy * fy + fz * fz;
+  const float rsf = xif.w + xjf.w;
+  const float cutf = adh ? rsf * 1.5f : rsf;
+  const float X = fmaxf(Xi, fmaxf(fmaxf(fabsf(xjf.x), fabsf(xjf.y)), fabsf(xjf.z)));
+  const float e = 6.0e-8f * (2.0f * X + 2.0f * cutf + P.lmax);
+  const float band = 4.1f * cutf * e + 3.0f * e * e + 1.0e-6f * cutf * cutf;
+  return d2f > cutf * cutf + band;
+}
+
+__device__ __forceinline__ V mic(const StepParams& P, V d) {
+  if (P.periodic[0]) { if (d.x > P.bsize[0] * 0.5) d.x = d.x - P.bsize[0]; else if (d.x < -P.bsize[0] * 0.5) d.x = d.x + P.bsize[0]; }
+  if (P.periodic[1]) { if (d.y > P.bsize[1] * 0.5) d.y = d.y - P.bsize[1]; else if (d.y < -P.bsize[1] * 0.5) d.y = d.y + P.bsize[1]; }
+  if (P.periodic[2]) { if (d.z > P.bsize[2] * 0.5) d.z = d.z - P.bsize[2]; else if (d.z < -P.bsize[2] * 0.5) d.z = d.z + P.bsize[2]; }
+  return d;
+}
+
+// Pass 1: records (j, row position, visits both ways, d^2) of the contacts of
+// each particle; counts all records and the ones that evaluate their pair
+// (the lower slot of a pair seen from both ends, or the only end that sees it).
+template <bool PHYS, bool HIST>
+__global__ void __launch_bounds__(128) k_contact_filter(StepParams P) {
+  Ctrl* C = P.ctrl;
+  if (C->halt) return;
+  const Bank B = P.bank[C->bank];
+  const bool adh = (P.nmodel == 3 || P.nmodel == 4);
+  const size_t plane = (size_t)P.n * P.cap;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < P.n; k += gridDim.x * blockDim.x) {
+    uint32_t nrec = 0, ncmp = 0;
+    if (!(B.flags[k] & PF_DEAD)) {
+      const D4 xi4 = B.xr[k];
+      const V xi = xyz(xi4);
+      const double ri = xi4.w;
+      const unsigned long long ci = PHYS ? 0ull : (unsigned long long)__double_as_longlong(B.wc[k].w);
+      const float4 xif = B.xf[k];
+      const float Xi = fmaxf(fmaxf(fabsf(xif.x), fabsf(xif.y)), fabsf(xif.z));
+      const uint32_t cnt = B.ncnt[k];
+      const uint32_t* row = B.nbr + (size_t)k * P.cap;
+      CRec* out = P.crec + (size_t)k * P.cap;
+      for (uint32_t m = 0; m < cnt; ++m) {
+        const uint32_t j = row[m];
+        const size_t hi = (size_t)k * P.cap + m;
+        int vij = 0, vji = 0;
+        double d2 = 0.0;
+        if (!(P.pretest && pretest_far(P, xif, Xi, B.xf[j], adh))) {
+          const D4 xj4 = B.xr[j];
+          const V d = mic(P, xi - xyz(xj4));
+          d2 = dot(d, d);
+          const double rsum = ri + xj4.w;
+          const double cut = rsum + (adh ? rsum * 0.5 : 0.0);
+          if (d2 < cut * cut) {
+            if (PHYS) {
+              vij = vji = 1;
+            } else {
+              const unsigned long long cj = (unsigned long long)__double_as_longlong(B.wc[j].w);
+              vij = ref_visits(P, ci, cj);
+              vji = ref_visits(P, cj, ci);
+            }
+          }
+        }
+        if (vij > 0) {
+          out[nrec] = CRec{j, m | ((uint32_t)vij << 16) | ((uint32_t)vji << 24), d2};
+          ++nrec;
+          if (!(vji > 0 && (uint32_t)k > j)) ++ncmp;
+        } else if (HIST) {
+          B.hist[hi] = 0.0;
+          B.hist[plane + hi] = 0.0;
+          B.hist[2 * plane + hi] = 0.0;
+        }
+        if (P.debug) P.dbgMult[hi] = (uint8_t)vij;
+      }
+    }
+    P.ccnt[k] = nrec;
+    P.ncomp[k] = ncmp;
+  }
+}
+
+// Pass 2: the compact list of evaluating records.
+__global__ void __launch_bounds__(256) k_contact_index(StepParams P) {
+  if (P.ctrl->halt) return;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < P.n; k += gridDim.x * blockDim.x) {
+    const uint32_t n = P.ccnt[k];
+    uint32_t q = P.poff[k];
+    const size_t base = (size_t)k * P.cap;
+    for (uint32_t c = 0; c < n; ++c) {
+      const CRec r = P.crec[base + c];
+      if (!((r.mv >> 24) > 0 && (uint32_t)k > r.j)) P.clist[q++] = (uint32_t)(base + c);
+    }
+  }
+}
+
+// Pass 3: one thread per pair. The force on the row's particle times its
+// visit count goes to its result; the other end receives exactly the
+// negated force (the reference's formula is sign-symmetric: evaluated from
+// that end it gives -f bit for bit) times its own visit count, with its own
+// torque (n r_j) x (-f), and in physical mode the negated spring.
+template <bool PHYS, bool HIST, typename R>
+__global__ void __launch_bounds__(128) k_contact_force(StepParams P) {
+  Ctrl* C = P.ctrl;
+  if (C->halt) return;
+  const Bank B = P.bank[C->bank];
+  const size_t plane = (size_t)P.n * P.cap;
+  const uint32_t total = P.ctot[1];
+  bool excess = false;
+  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+    const uint32_t s = P.clist[t];
+    const uint32_t k = s / (uint32_t)P.cap, c = s - k * (uint32_t)P.cap;
+    const CRec r = P.crec[s];
+    const uint32_t j = r.j, m = r.mv & 0xFFFFu;
+    const int vij = (r.mv >> 16) & 0xFF, vji = r.mv >> 24;
+    const D4 xi4 = B.xr[k], vi4 = B.vm[k], wi4 = B.wc[k];
+    const D4 xj4 = B.xr[j], vj4 = B.vm[j], wj4 = B.wc[j];
+    const V d = mic(P, xyz(xi4) - xyz(xj4));
+    const double rsum = xi4.w + xj4.w;
+    double* hk = HIST ? B.hist + ((size_t)k * P.cap + m) : nullptr;
+    V fc, tc, nrm;
+    if (!pair_contact<R, PHYS, HIST>(P, d, r.d2, rsum, xi4.w, xj4.w, vi4.w, vj4.w, xyz(vi4), xyz(vj4), xyz(wi4),
+                                     xyz(wj4), hk, plane, fc, tc, nrm, excess))
+      pair_contact<double, PHYS, HIST>(P, d, r.d2, rsum, xi4.w, xj4.w, vi4.w, vj4.w, xyz(vi4), xyz(vj4), xyz(wi4),
+                                       xyz(wj4), hk, plane, fc, tc, nrm, excess);
+    double* out = P.cres + 6 * (size_t)(P.coff[k] + c);
+    const double sv = (double)vij;
+    out[0] = fc.x * sv; out[1] = fc.y * sv; out[2] = fc.z * sv;
+    out[3] = tc.x * sv; out[4] = tc.y * sv; out[5] = tc.z * sv;
+    if (vji > 0) {
+      const uint32_t nj = P.ccnt[j];
+      const CRec* rj = P.crec + (size_t)j * P.cap;
+      for (uint32_t c2 = 0; c2 < nj; ++c2) {
+        if (rj[c2].j != k) continue;
+        const V f2 = -fc;
+        V t2;
+        if (sizeof(R) == sizeof(float)) {
+          const Vf raj = cvt<float>(nrm) * (float)xj4.w;
+          t2 = cvt<double>(cross(raj, cvt<float>(f2)));
+        } else {
+          t2 = cross(nrm * xj4.w, f2);
+        }
+        double* o2 = P.cres + 6 * (size_t)(P.coff[j] + c2);
+        const double s2 = (double)vji;
+        o2[0] = f2.x * s2; o2[1] = f2.y * s2; o2[2] = f2.z * s2;
+        o2[3] = t2.x * s2; o2[4] = t2.y * s2; o2[5] = t2.z * s2;
+        if (HIST) {
+          const size_t h2 = (size_t)j * P.cap + (rj[c2].mv & 0xFFFFu);
+          B.hist[h2] = -hk[0];
+          B.hist[plane + h2] = -hk[plane];
+          B.hist[2 * plane + h2] = -hk[2 * plane];
+        }
+        break;
+      }
+    }
+  }
+  if (excess) C->overlap_flag = 1;
+}
+
+// Pass 4: per particle, the contact results in list order, the walls, then
+// a = g + F/m and tau = T (src/simulation.rs:265-271, 532-536).
+__global__ void __launch_bounds__(128) k_accumulate(StepParams P) {
+  Ctrl* C = P.ctrl;
+  if (C->halt) return;
+  const Bank B = P.bank[C->bank];
+  bool excess = false;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < P.n; k += gridDim.x * blockDim.x) {
+    if (B.flags[k] & PF_DEAD) continue;
+    V F = vmk(0.0, 0.0, 0.0), T = vmk(0.0, 0.0, 0.0);
+    const uint32_t n = P.ccnt[k];
+    const double* res = P.cres + 6 * (size_t)P.coff[k];
+    for (uint32_t c = 0; c < n; ++c) {
+      F = F + vmk(res[6 * c], res[6 * c + 1], res[6 * c + 2]);
+      T = T + vmk(res[6 * c + 3], res[6 * c + 4], res[6 * c + 5]);
+    }
+    const D4 xi4 = B.xr[k], vi4 = B.vm[k], wi4 = B.wc[k];
+    const double mi = vi4.w;
+    if (P.ntri > 0) wall_forces(P, xyz(xi4), xyz(vi4), xyz(wi4), xi4.w, mi, P.beta_abs, F, T, excess);
+    if (P.debug) {
+      P.dbgF[3 * (size_t)k] = F.x; P.dbgF[3 * (size_t)k + 1] = F.y; P.dbgF[3 * (size_t)k + 2] = F.z;
+      P.dbgT[3 * (size_t)k] = T.x; P.dbgT[3 * (size_t)k + 1] = T.y; P.dbgT[3 * (size_t)k + 2] = T.z;
+    }
+    if (!isfinite(F.x + F.y + F.z + T.x + T.y + T.z)) atomicOr(&C->status, (unsigned)ST_NAN);
     const V a = vmk(P.gravity[0], P.gravity[1], P.gravity[2]) + F / mi;
     const V tau = vmk(0.0, 0.0, 0.0) + T;
     B.acc[k] = D4{a.x, a.y, a.z, 0.0};
@@ -658,8 +866,27 @@ static void launch_force_t(const StepParams& P, int g, cudaStream_t s) {
   else k_force<true, false, R><<<g, 128, 0, s>>>(P);
 }
 
+template <typename R>
+static int launch_contact_path(const StepParams& P, cudaStream_t s) {
+  const int g = grid_for(P.n, 128);
+  const bool hist = P.mode == 1 && P.tmodel != 0;
+  if (P.mode == 0) k_contact_filter<false, false><<<g, 128, 0, s>>>(P);
+  else if (hist) k_contact_filter<true, true><<<g, 128, 0, s>>>(P);
+  else k_contact_filter<true, false><<<g, 128, 0, s>>>(P);
+  launch_exclusive_scan(nullptr, P.ccnt, P.coff, (uint32_t)P.n, P.cpart, P.ctot, s);
+  launch_exclusive_scan(nullptr, P.ncomp, P.poff, (uint32_t)P.n, P.cpart, P.ctot + 1, s);
+  k_contact_index<<<grid_for(P.n, 256), 256, 0, s>>>(P);
+  const int gc = grid_for((uint64_t)P.n * 4, 128);
+  if (P.mode == 0) k_contact_force<false, false, R><<<gc, 128, 0, s>>>(P);
+  else if (hist) k_contact_force<true, true, R><<<gc, 128, 0, s>>>(P);
+  else k_contact_force<true, false, R><<<gc, 128, 0, s>>>(P);
+  k_accumulate<<<g, 128, 0, s>>>(P);
+  return 10;
+}
+
 int launch_force(const StepParams& P, cudaStream_t s) {
   if (P.n == 0) return 0;
+  if (P.force_path == 0) return P.prec == 1 ? launch_contact_path<float>(P, s) : launch_contact_path<double>(P, s);
   const int g = grid_for(P.n, 128);
   if (P.prec == 1) launch_force_t<float>(P, g, s);
   else launch_force_t<double>(P, g, s);

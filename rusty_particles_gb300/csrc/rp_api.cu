@@ -460,6 +460,17 @@ int rp_set_neighbor_capacity(rp_sim* s, int capacity) {
   return RP_OK;
 }
 
+int rp_set_force_path(rp_sim* s, int path) {
+  SIM_OR_FAIL(s);
+  if (path != 0 && path != 1) {
+    set_error("force path must be 0 or 1");
+    return RP_E_INVALID_ARG;
+  }
+  s->e->force_path = path;
+  s->e->config_changed();
+  return RP_OK;
+}
+
 int rp_set_device_loop(rp_sim* s, int enable) {
   SIM_OR_FAIL(s);
   s->e->use_graph_ = enable != 0;

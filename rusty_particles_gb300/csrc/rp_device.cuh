@@ -70,9 +70,28 @@ struct TriRec {
   double a, b, c, det, denom, pad;
 };
 
+// A contact found by the filter: neighbour slot, row position and the
+// reference's visit counts from both ends (m | vis_ij << 16 | vis_ji << 24).
+struct CRec {
+  uint32_t j;
+  uint32_t mv;
+  double d2;
+};
+
 struct StepParams {
   int n;  // slots
   int cap;
+  int force_path;  // 0: contact-parallel (default), 1: one thread per particle
+  // contact-parallel buffers (recomputed every step)
+  CRec* crec;       // n*cap records, row k at k*cap
+  uint32_t* ccnt;   // records per particle
+  uint32_t* ncomp;  // records that evaluate their pair (each pair once)
+  uint32_t* coff;   // exclusive scan of ccnt: result offset of particle k
+  uint32_t* poff;   // exclusive scan of ncomp
+  uint32_t* clist;  // compact list of evaluating record slots
+  uint32_t* ctot;   // [0] records, [1] evaluating records
+  double* cres;     // per record: force (3) and torque (3) on the row's particle
+  uint32_t* cpart;  // scan partials
   int nmodel, tmodel, mode, prec;
   int periodic[3];
   int debug;

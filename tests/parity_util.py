@@ -65,8 +65,9 @@ def oracle_sim(oracle_mod, st, dt, lo, hi, normal, tangential, periodic=(False, 
 
 
 def gpu_sim(rp, st, dt, lo, hi, normal, tangential, periodic=(False, False, False), mode=0,
-            material=(1e7, 0.3, 2500.0, 0.5, 0.5, 0.0), wall=None, tris=None, cell=1.0, precision=0):
+            material=(1e7, 0.3, 2500.0, 0.5, 0.5, 0.0), wall=None, tris=None, cell=1.0, precision=0, force_path=0):
     s = rp.Simulation.create(dt, lo[0], lo[1], lo[2], hi[0], hi[1], hi[2], len(st["radius"]))
+    s._L.rp_set_force_path(s._h, force_path)
     s.set_interaction_mode(mode)
     s.set_precision(precision)
     s.set_reference_cell_size(cell)

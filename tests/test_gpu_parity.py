@@ -141,6 +141,21 @@ def test_one_step_physical_mindlin(rp, oracle_mod):
     assert np.max(np.abs(sg["position"] - so["x"])) < 1e-12
 
 
+@pytest.mark.parametrize("mode,tangential,periodic", [(0, 0, (False, False, False)), (0, 2, (True, False, True)),
+                                                      (1, 2, (False, False, False)), (1, 0, (True, True, True))])
+def test_force_paths_agree(rp, oracle_mod, mode, tangential, periodic):
+    # the per-particle path and the contact-parallel path (each pair once,
+    # +-f) give the oracle's forces, and each other's to rounding
+    lo, hi = (-0.3, -0.3, -0.3), (0.3, 0.3, 0.3)
+    st = pu.random_bed(500 + mode, 3000, lo, hi, 0.008, 0.012)
+    for path in (0, 1):
+        o = pu.oracle_sim(oracle_mod, st, 1e-5, lo, hi, 1, tangential, periodic, mode)
+        g = pu.gpu_sim(rp, st, 1e-5, lo, hi, 1, tangential, periodic, mode, force_path=path)
+        o.step()
+        g.step()
+        compare_step(o, g)
+
+
 @pytest.mark.parametrize("normal", [0, 1, 2, 3, 4])
 def test_mixed_precision_one_step(rp, oracle_mod, normal):
     # FP32 pair math on FP64 differences: cutoff decisions, contact set and
