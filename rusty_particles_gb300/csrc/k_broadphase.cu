@@ -315,7 +315,9 @@ __global__ void k_build_nlist(StepParams P, const uint32_t* cstart, const uint32
       continue;
     }
     const D4 xi = B.xr[k];
-    const float ri = (float)xi.w;
+    const float4 xif = B.xf[k];
+    const float ri = xif.w;
+    const float Xi = fmaxf(fmaxf(fabsf(xif.x), fabsf(xif.y)), fabsf(xif.z));
     uint32_t cl = fine_cell(P, xi.x, xi.y, xi.z);
     int c[3];
     c[0] = (int)(cl % (uint32_t)P.fdims[0]);
@@ -352,15 +354,18 @@ __global__ void k_build_nlist(StepParams P, const uint32_t* cstart, const uint32
           uint32_t e = cend[cell];
           for (uint32_t j = s; j < e; ++j) {
             if ((int)j == k) continue;
-            const D4 xj = B.xr[j];
-            double d[3] = {xi.x - xj.x, xi.y - xj.y, xi.z - xj.z};
-#pragma unroll
-            for (int a = 0; a < 3; ++a)
-              if (P.periodic[a]) d[a] -= P.bsize[a] * rint(d[a] / P.bsize[a]);
-            float fx = (float)d[0], fy = (float)d[1], fz = (float)d[2];
+            // FP32 on the position mirror: each difference is within
+            // 2^-24 (2X + |d| + L) of the exact one, so growing the radius by
+            // 2.5e-7 (2X + L) + a relative 1e-5 keeps the list a superset
+            const float4 xj = B.xf[j];
+            float fx = xif.x - xj.x, fy = xif.y - xj.y, fz = xif.z - xj.z;
+            if (P.periodic[0]) fx -= (float)P.bsize[0] * rintf(fx / (float)P.bsize[0]);
+            if (P.periodic[1]) fy -= (float)P.bsize[1] * rintf(fy / (float)P.bsize[1]);
+            if (P.periodic[2]) fz -= (float)P.bsize[2] * rintf(fz / (float)P.bsize[2]);
             float d2 = fx * fx + fy * fy + fz * fz;
-            float rl = (ri + (float)xj.w) * adh + skin;
-            rl *= P.list_scale;
+            const float X = fmaxf(Xi, fmaxf(fmaxf(fabsf(xj.x), fabsf(xj.y)), fabsf(xj.z)));
+            float rl = (ri + xj.w) * adh + skin;
+            rl = rl * P.list_scale + 2.5e-7f * (2.0f * X + P.lmax);
             if (d2 < rl * rl) {
               if (cnt < (uint32_t)P.cap) {
                 row[cnt] = j;
