@@ -413,7 +413,12 @@ int Engine::build_triangle_grid(double rmax) {
   std::vector<TriRec> recs(T);
   double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
   std::vector<double> blo(3 * T), bhi(3 * T);
-  const double grow = rmax * (1.0 + 1e-9) + 1e-12;
+  // Cells are looked up in FP32 on the device (error ~1e-7 of the coordinate),
+  // so bounding boxes grow by the largest radius plus an absolute margin that
+  // covers a lookup landing in a neighbouring cell.
+  double extent_abs = 0.0;
+  for (float q : tri_v_) extent_abs = std::max(extent_abs, std::fabs((double)q));
+  const double grow = rmax * (1.0 + 1e-6) + 1e-6 * (1.0 + extent_abs + rmax);
   for (size_t t = 0; t < T; ++t) {
     const float* q = &tri_v_[9 * t];
     TriRec& r = recs[t];
@@ -430,6 +435,21 @@ int Engine::build_triangle_grid(double rmax) {
     r.det = r.a * r.c - r.b * r.b;
     r.denom = r.a - 2.0 * r.b + r.c;
     r.pad = 0.0;
+    {
+      double cx = r.e0[1] * r.e1[2] - r.e0[2] * r.e1[1], cy = r.e0[2] * r.e1[0] - r.e0[0] * r.e1[2],
+             cz = r.e0[0] * r.e1[1] - r.e0[1] * r.e1[0];
+      double l = std::sqrt(cx * cx + cy * cy + cz * cz);
+      if (l > 0.0 && std::isfinite(l)) {
+        cx /= l; cy /= l; cz /= l;
+        r.plane = make_float4((float)cx, (float)cy, (float)cz, (float)(cx * v0[0] + cy * v0[1] + cz * v0[2]));
+      } else {
+        r.plane = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+      double vm = 0.0;
+      for (int k = 0; k < 3; ++k)
+        vm = std::max(vm, std::max(std::fabs(v0[k]), std::max(std::fabs(v1[k]), std::fabs(v2[k]))));
+      r.bound = make_float4((float)vm, 0.f, 0.f, 0.f);
+    }
     for (int k = 0; k < 3; ++k) {
       double mn = std::min(v0[k], std::min(v1[k], v2[k])) - grow;
       double mx = std::max(v0[k], std::max(v1[k], v2[k])) + grow;
@@ -496,9 +516,11 @@ int Engine::build_triangle_grid(double rmax) {
   P_.titems = titems_d_;
   for (int k = 0; k < 3; ++k) {
     P_.tmin[k] = lo[k];
+    P_.tminf[k] = (float)lo[k];
     P_.tdims[k] = dims[k];
   }
   P_.tcell = cell;
+  P_.tinvf = (float)(1.0 / cell);
   return RP_OK;
 }
 

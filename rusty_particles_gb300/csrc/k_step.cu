@@ -421,18 +421,29 @@ __global__ void __launch_bounds__(256) k_second_half(StepParams P) {
 
 // Wall contacts of one particle (src/simulation.rs:464-523): the triangles
 // listed in the triangle-grid cell of its centre, in mesh order.
-__device__ __forceinline__ void wall_forces(const StepParams& P, V xi, V vi, V wi, double ri, double mi,
+// The cell lookup runs in FP32 on the position mirror (the host grows every
+// triangle's box by a margin covering the FP32 error), and a triangle whose
+// plane is farther than the radius (plus rounding) cannot touch the sphere,
+// because the closest point lies in that plane: both skip FP64 work only.
+__device__ __forceinline__ void wall_forces(const StepParams& P, V xi, float4 xf, V vi, V wi, double ri, double mi,
                                             double beta_abs, V& F, V& T, bool& excess) {
   if (P.ntri > 0) {
-    const double q0 = floor((xi.x - P.tmin[0]) / P.tcell);
-    const double q1 = floor((xi.y - P.tmin[1]) / P.tcell);
-    const double q2 = floor((xi.z - P.tmin[2]) / P.tcell);
-    if (q0 >= 0.0 && q1 >= 0.0 && q2 >= 0.0 && q0 < (double)P.tdims[0] && q1 < (double)P.tdims[1] &&
-        q2 < (double)P.tdims[2]) {
+    const float q0 = floorf((xf.x - P.tminf[0]) * P.tinvf);
+    const float q1 = floorf((xf.y - P.tminf[1]) * P.tinvf);
+    const float q2 = floorf((xf.z - P.tminf[2]) * P.tinvf);
+    if (q0 >= 0.f && q1 >= 0.f && q2 >= 0.f && q0 < (float)P.tdims[0] && q1 < (float)P.tdims[1] &&
+        q2 < (float)P.tdims[2]) {
       const uint32_t cell = (uint32_t)q0 + (uint32_t)P.tdims[0] * ((uint32_t)q1 + (uint32_t)P.tdims[1] * (uint32_t)q2);
       const uint32_t s = P.tstart[cell], e = P.tstart[cell + 1];
+      const float rf = (float)ri;
+      const float xmag = fmaxf(fmaxf(fabsf(xf.x), fabsf(xf.y)), fabsf(xf.z));
       for (uint32_t t = s; t < e; ++t) {
         const TriRec& tr = P.tri[P.titems[t]];
+        // FP32 rounding of n, n.v0 and x moves n.x - n.v0 by at most
+        // ~3e-7 (|x| + |n.v0|) + 1.1e-7 |x - v0|; the margin is larger
+        const float4 pl = tr.plane;
+        const float hd = fabsf(pl.x * xf.x + pl.y * xf.y + pl.z * xf.z - pl.w);
+        if (hd > rf + 1e-6f * (1.0f + xmag + fabsf(pl.w) + rf) + 2e-7f * (xmag + tr.bound.x)) continue;
         // closest point, src/mesh.rs:45-117 (same regions and clamps)
         const V v0 = vmk(tr.v0[0] - xi.x, tr.v0[1] - xi.y, tr.v0[2] - xi.z);
         const V e0 = vmk(tr.e0[0], tr.e0[1], tr.e0[2]), e1 = vmk(tr.e1[0], tr.e1[1], tr.e1[2]);
@@ -580,7 +591,7 @@ __global__ void __launch_bounds__(128) k_force(StepParams P) {
       }
       if (P.debug) P.dbgMult[hi] = (uint8_t)visits;
     }
-    wall_forces(P, xi, vi, wi, ri, mi, beta_abs, F, T, excess);
+    wall_forces(P, xi, xif, vi, wi, ri, mi, beta_abs, F, T, excess);
     if (P.debug) {
       P.dbgF[3 * (size_t)k] = F.x; P.dbgF[3 * (size_t)k + 1] = F.y; P.dbgF[3 * (size_t)k + 2] = F.z;
       P.dbgT[3 * (size_t)k] = T.x; P.dbgT[3 * (size_t)k + 1] = T.y; P.dbgT[3 * (size_t)k + 2] = T.z;
@@ -628,9 +639,12 @@ __device__ __forceinline__ V mic(const StepParams& P, V d) {
   return d;
 }
 
-// Pass 1: records (j, row position, visits both ways, d^2) of the contacts of
-// each particle; counts all records and the ones that evaluate their pair
-// (the lower slot of a pair seen from both ends, or the only end that sees it).
+// Pass 1 (FP32 and integer work only): the candidates of each particle, i.e.
+// list entries the FP32 pretest cannot rule out and that the reference's loop
+// visits from this end (visit counts from both ends recorded); counts all
+// candidates and the ones that evaluate their pair (the lower slot of a pair
+// seen from both ends, or the only end that sees it). The pretest is
+// symmetric, so a pair seen from both ends is a candidate at both.
 template <bool PHYS, bool HIST>
 __global__ void __launch_bounds__(128) k_contact_filter(StepParams P) {
   Ctrl* C = P.ctrl;
@@ -641,9 +655,6 @@ __global__ void __launch_bounds__(128) k_contact_filter(StepParams P) {
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < P.n; k += gridDim.x * blockDim.x) {
     uint32_t nrec = 0, ncmp = 0;
     if (!(B.flags[k] & PF_DEAD)) {
-      const D4 xi4 = B.xr[k];
-      const V xi = xyz(xi4);
-      const double ri = xi4.w;
       const unsigned long long ci = PHYS ? 0ull : (unsigned long long)__double_as_longlong(B.wc[k].w);
       const float4 xif = B.xf[k];
       const float Xi = fmaxf(fmaxf(fabsf(xif.x), fabsf(xif.y)), fabsf(xif.z));
@@ -654,33 +665,27 @@ __global__ void __launch_bounds__(128) k_contact_filter(StepParams P) {
         const uint32_t j = row[m];
         const size_t hi = (size_t)k * P.cap + m;
         int vij = 0, vji = 0;
-        double d2 = 0.0;
         if (!(P.pretest && pretest_far(P, xif, Xi, B.xf[j], adh))) {
-          const D4 xj4 = B.xr[j];
-          const V d = mic(P, xi - xyz(xj4));
-          d2 = dot(d, d);
-          const double rsum = ri + xj4.w;
-          const double cut = rsum + (adh ? rsum * 0.5 : 0.0);
-          if (d2 < cut * cut) {
-            if (PHYS) {
-              vij = vji = 1;
-            } else {
-              const unsigned long long cj = (unsigned long long)__double_as_longlong(B.wc[j].w);
-              vij = ref_visits(P, ci, cj);
-              vji = ref_visits(P, cj, ci);
-            }
+          if (PHYS) {
+            vij = vji = 1;
+          } else {
+            const unsigned long long cj = (unsigned long long)__double_as_longlong(B.wc[j].w);
+            vij = ref_visits(P, ci, cj);
+            vji = ref_visits(P, cj, ci);
           }
         }
         if (vij > 0) {
-          out[nrec] = CRec{j, m | ((uint32_t)vij << 16) | ((uint32_t)vji << 24), d2};
+          out[nrec] = CRec{j, m | ((uint32_t)vij << 16) | ((uint32_t)vji << 24)};
           ++nrec;
           if (!(vji > 0 && (uint32_t)k > j)) ++ncmp;
-        } else if (HIST) {
-          B.hist[hi] = 0.0;
-          B.hist[plane + hi] = 0.0;
-          B.hist[2 * plane + hi] = 0.0;
+        } else {
+          if (HIST) {
+            B.hist[hi] = 0.0;
+            B.hist[plane + hi] = 0.0;
+            B.hist[2 * plane + hi] = 0.0;
+          }
+          if (P.debug) P.dbgMult[hi] = 0;
         }
-        if (P.debug) P.dbgMult[hi] = (uint8_t)vij;
       }
     }
     P.ccnt[k] = nrec;
@@ -702,11 +707,13 @@ __global__ void __launch_bounds__(256) k_contact_index(StepParams P) {
   }
 }
 
-// Pass 3: one thread per pair. The force on the row's particle times its
-// visit count goes to its result; the other end receives exactly the
-// negated force (the reference's formula is sign-symmetric: evaluated from
-// that end it gives -f bit for bit) times its own visit count, with its own
-// torque (n r_j) x (-f), and in physical mode the negated spring.
+// Pass 3: one thread per candidate pair: the exact FP64 cutoff test of
+// src/simulation.rs:343-357, then the pair laws. The force on the row's
+// particle times its visit count goes to its result; the other end receives
+// exactly the negated force (the reference's formula is sign-symmetric:
+// evaluated from that end it gives -f bit for bit) times its own visit count,
+// with its own torque (n r_j) x (-f), and in physical mode the negated spring.
+// A candidate outside the cutoff gives zero results at both ends.
 template <bool PHYS, bool HIST, typename R>
 __global__ void __launch_bounds__(128) k_contact_force(StepParams P) {
   Ctrl* C = P.ctrl;
@@ -714,6 +721,7 @@ __global__ void __launch_bounds__(128) k_contact_force(StepParams P) {
   const Bank B = P.bank[C->bank];
   const size_t plane = (size_t)P.n * P.cap;
   const uint32_t total = P.ctot[1];
+  const bool adh = (P.nmodel == 3 || P.nmodel == 4);
   bool excess = false;
   for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
     const uint32_t s = P.clist[t];
@@ -721,16 +729,27 @@ __global__ void __launch_bounds__(128) k_contact_force(StepParams P) {
     const CRec r = P.crec[s];
     const uint32_t j = r.j, m = r.mv & 0xFFFFu;
     const int vij = (r.mv >> 16) & 0xFF, vji = r.mv >> 24;
-    const D4 xi4 = B.xr[k], vi4 = B.vm[k], wi4 = B.wc[k];
-    const D4 xj4 = B.xr[j], vj4 = B.vm[j], wj4 = B.wc[j];
+    const D4 xi4 = B.xr[k], xj4 = B.xr[j];
     const V d = mic(P, xyz(xi4) - xyz(xj4));
+    const double d2 = dot(d, d);
     const double rsum = xi4.w + xj4.w;
-    double* hk = HIST ? B.hist + ((size_t)k * P.cap + m) : nullptr;
-    V fc, tc, nrm;
-    if (!pair_contact<R, PHYS, HIST>(P, d, r.d2, rsum, xi4.w, xj4.w, vi4.w, vj4.w, xyz(vi4), xyz(vj4), xyz(wi4),
-                                     xyz(wj4), hk, plane, fc, tc, nrm, excess))
-      pair_contact<double, PHYS, HIST>(P, d, r.d2, rsum, xi4.w, xj4.w, vi4.w, vj4.w, xyz(vi4), xyz(vj4), xyz(wi4),
-                                       xyz(wj4), hk, plane, fc, tc, nrm, excess);
+    const double cut = rsum + (adh ? rsum * 0.5 : 0.0);
+    const bool in = d2 < cut * cut;
+    const size_t hik = (size_t)k * P.cap + m;
+    double* hk = HIST ? B.hist + hik : nullptr;
+    V fc = vmk(0.0, 0.0, 0.0), tc = fc, nrm = fc;
+    if (in) {
+      const D4 vi4 = B.vm[k], wi4 = B.wc[k], vj4 = B.vm[j], wj4 = B.wc[j];
+      if (!pair_contact<R, PHYS, HIST>(P, d, d2, rsum, xi4.w, xj4.w, vi4.w, vj4.w, xyz(vi4), xyz(vj4), xyz(wi4),
+                                       xyz(wj4), hk, plane, fc, tc, nrm, excess))
+        pair_contact<double, PHYS, HIST>(P, d, d2, rsum, xi4.w, xj4.w, vi4.w, vj4.w, xyz(vi4), xyz(vj4), xyz(wi4),
+                                         xyz(wj4), hk, plane, fc, tc, nrm, excess);
+    } else if (HIST) {
+      hk[0] = 0.0;
+      hk[plane] = 0.0;
+      hk[2 * plane] = 0.0;
+    }
+    if (P.debug) P.dbgMult[hik] = (uint8_t)(in ? vij : 0);
     double* out = P.cres + 6 * (size_t)(P.coff[k] + c);
     const double sv = (double)vij;
     out[0] = fc.x * sv; out[1] = fc.y * sv; out[2] = fc.z * sv;
@@ -752,12 +771,13 @@ __global__ void __launch_bounds__(128) k_contact_force(StepParams P) {
         const double s2 = (double)vji;
         o2[0] = f2.x * s2; o2[1] = f2.y * s2; o2[2] = f2.z * s2;
         o2[3] = t2.x * s2; o2[4] = t2.y * s2; o2[5] = t2.z * s2;
+        const size_t h2 = (size_t)j * P.cap + (rj[c2].mv & 0xFFFFu);
         if (HIST) {
-          const size_t h2 = (size_t)j * P.cap + (rj[c2].mv & 0xFFFFu);
           B.hist[h2] = -hk[0];
           B.hist[plane + h2] = -hk[plane];
           B.hist[2 * plane + h2] = -hk[2 * plane];
         }
+        if (P.debug) P.dbgMult[h2] = (uint8_t)(in ? vji : 0);
         break;
       }
     }
@@ -783,7 +803,7 @@ __global__ void __launch_bounds__(128) k_accumulate(StepParams P) {
     }
     const D4 xi4 = B.xr[k], vi4 = B.vm[k], wi4 = B.wc[k];
     const double mi = vi4.w;
-    if (P.ntri > 0) wall_forces(P, xyz(xi4), xyz(vi4), xyz(wi4), xi4.w, mi, P.beta_abs, F, T, excess);
+    if (P.ntri > 0) wall_forces(P, xyz(xi4), B.xf[k], xyz(vi4), xyz(wi4), xi4.w, mi, P.beta_abs, F, T, excess);
     if (P.debug) {
       P.dbgF[3 * (size_t)k] = F.x; P.dbgF[3 * (size_t)k + 1] = F.y; P.dbgF[3 * (size_t)k + 2] = F.z;
       P.dbgT[3 * (size_t)k] = T.x; P.dbgT[3 * (size_t)k + 1] = T.y; P.dbgT[3 * (size_t)k + 2] = T.z;

@@ -68,14 +68,15 @@ struct Bank {
 struct TriRec {
   double v0[3], e0[3], e1[3], n[3];
   double a, b, c, det, denom, pad;
+  float4 plane;  // unit normal from the vertices and n.v0, FP32 (zero for a degenerate triangle)
+  float4 bound;  // .x = largest |vertex coordinate| (scales the FP32 plane-test error)
 };
 
-// A contact found by the filter: neighbour slot, row position and the
-// reference's visit counts from both ends (m | vis_ij << 16 | vis_ji << 24).
+// A contact candidate kept by the filter: neighbour slot, row position and
+// the reference's visit counts from both ends (m | vis_ij << 16 | vis_ji << 24).
 struct CRec {
   uint32_t j;
   uint32_t mv;
-  double d2;
 };
 
 struct StepParams {
@@ -117,6 +118,7 @@ struct StepParams {
   int ntri;
   const TriRec* tri;
   double tmin[3], tcell;
+  float tminf[3], tinvf;  // FP32 lookup: cell = floor((x - tmin) * (1/tcell))
   int tdims[3];
   const uint32_t* tstart;
   const uint32_t* titems;
