@@ -165,6 +165,44 @@ def box_workload(seed=7):
     }
 
 
+def adhesive_workload(n=4_194_304, seed=2027, phi=0.35):
+    """Adhesive gas: n spheres, radii U[5, 20] um, JKR + Coulomb, E = 5e8 Pa,
+    nu = 0.25, surface energy 0.05 J/m^2, rho = 2000 kg/m^3, in a periodic cube
+    at solid fraction 0.35 with Gaussian velocities (sigma 0.05 m/s per axis),
+    dt = 1e-8 s. Start: a shuffled cubic lattice at 0.6x radii grown to full
+    size by `relax` (no overlaps at the start of the timed run)."""
+    rng = np.random.default_rng(seed)
+    r = rng.uniform(5e-6, 20e-6, n)
+    rho = 2000.0
+    L = (float((4.0 / 3.0 * np.pi * r ** 3).sum()) / phi) ** (1.0 / 3.0)
+    m = math.ceil(n ** (1.0 / 3.0))
+    s = L / m
+    g = np.stack(np.meshgrid(*[np.arange(m)] * 3, indexing="ij"), -1).reshape(-1, 3)
+    g = g[rng.permutation(len(g))[:n]]
+    g = g[np.lexsort((g[:, 2], g[:, 1], g[:, 0]))]
+    x = (g + 0.5) * s + rng.uniform(-0.05, 0.05, g.shape) * s
+    return {
+        "name": "adhesive-4M" if n == 4_194_304 else f"adhesive-{n}",
+        "lo": (0.0, 0.0, 0.0), "hi": (L, L, L), "periodic": (True, True, True),
+        "dt": 1e-8, "normal": "jkr", "tangential": "coulomb",
+        "material": (5e8, 0.25, rho, 0.5, 0.5, 0.05),
+        "tri_v": np.zeros((0, 9), np.float32), "tri_n": np.zeros((0, 3), np.float32),
+        "position": x, "radius": r, "mass": rho * 4.0 / 3.0 * np.pi * r ** 3,
+        "velocity": rng.normal(0.0, 0.05, (n, 3)),
+        "describe": (f"{n:,} spheres, radii U[5,20] um, JKR+Coulomb, E=5e8 Pa, nu=0.25, gamma=0.05 J/m^2, "
+                     f"rho=2000, periodic cube L={L * 1e3:.3f} mm at solid fraction {phi}, Gaussian velocities "
+                     "(sigma 0.05 m/s), dt=1e-8 s"),
+    }
+
+
+def make_workload(args):
+    if args.workload == "hopper":
+        return hopper_workload(n=args.particles or 1_048_576)
+    if args.workload == "adhesive":
+        return adhesive_workload(n=args.particles or 4_194_304)
+    return box_workload()
+
+
 def make_sim(rp, wl, mode="parity", precision="fp64"):
     lo, hi = wl["lo"], wl["hi"]
     s = rp.Simulation.create(wl["dt"], lo[0], lo[1], lo[2], hi[0], hi[1], hi[2], len(wl["radius"]))
@@ -173,24 +211,30 @@ def make_sim(rp, wl, mode="parity", precision="fp64"):
     s.set_particle_material(*wl["material"])
     s.set_contact_models(wl["normal"], wl["tangential"])
     s.set_periodic_boundary(*wl["periodic"])
-    s.add_triangles(wl["tri_v"], wl["tri_n"])
+    if len(wl["tri_v"]):
+        s.add_triangles(wl["tri_v"], wl["tri_n"])
     s.add_particles(wl["position"], wl["radius"], wl["mass"])
+    if "velocity" in wl:
+        s.set_state({"velocity": wl["velocity"]})
     return s
 
 
 def relax(rp, wl, stages=9, steps_per_stage=100, settle=300, log=None):
     """Grow radii from 0.6x to 1x in stages while a damped, frictionless,
-    gravity-free run removes the overlaps; updates wl["position"] in place."""
+    gravity-free run removes the overlaps; updates wl["position"] in place.
+    The time step scales with the smallest radius (1e-5 s at 1 mm)."""
     x = wl["position"].copy()
     r, m = wl["radius"], wl["mass"]
     lo, hi = wl["lo"], wl["hi"]
-    s = rp.Simulation.create(1e-5, lo[0], lo[1], lo[2], hi[0], hi[1], hi[2], len(r))
+    dt = 1e-5 * float(np.min(r)) / 1e-3
+    s = rp.Simulation.create(dt, lo[0], lo[1], lo[2], hi[0], hi[1], hi[2], len(r))
     s.set_interaction_mode("parity")
     s.set_particle_material(1e7, 0.3, 2500.0, 0.0, 0.05, 0.0)
     s.set_contact_models("hertz", "coulomb")
     s.set_periodic_boundary(*wl["periodic"])
     s.set_gravity(0.0, 0.0, 0.0)
-    s.add_triangles(wl["tri_v"], wl["tri_n"])
+    if len(wl["tri_v"]):
+        s.add_triangles(wl["tri_v"], wl["tri_n"])
     s.add_particles(x, r * 0.6, m * 0.216)
     t0 = time.time()
     for k, f in enumerate(np.linspace(0.6, 1.0, stages)):
@@ -352,7 +396,10 @@ def run_oracle_sample(wl, idx, steps, threads):
     for i in idx:
         p = wl["position"][i]
         o.add_particle(p[0], p[1], p[2], wl["radius"][i], wl["mass"][i])
-    o.add_triangles(wl["tri_v"].astype(np.float64), wl["tri_n"].astype(np.float64))
+    if len(wl["tri_v"]):
+        o.add_triangles(wl["tri_v"].astype(np.float64), wl["tri_n"].astype(np.float64))
+    if "velocity" in wl:
+        o.set_state({"v": wl["velocity"][idx]})
     o.steps(1)  # warm-up (grid, contact map, page faults)
     t0 = time.perf_counter()
     o.steps(steps)
@@ -382,7 +429,7 @@ def run_reference(args, log):
     if rank != 0:
         barrier(dist)
         return 0
-    wl = hopper_workload() if args.workload == "hopper" else box_workload()
+    wl = make_workload(args)
     threads = os.cpu_count() or 1
     rates = []
     from oracle import oracle as om
@@ -419,11 +466,11 @@ def run_ours(args, log):
     import torch
     import rusty_particles_gb300 as rp
     torch.cuda.set_device(local)
-    wl = hopper_workload(n=args.particles) if args.workload == "hopper" else box_workload()
+    wl = make_workload(args)
     n = len(wl["radius"])
     if args.state_in:
         wl["position"] = np.load(args.state_in)["position"]
-    elif args.workload == "hopper":
+    elif args.workload in ("hopper", "adhesive"):
         relax(rp, wl, log=log)
     if args.state_out:
         np.savez(args.state_out, position=wl["position"])
@@ -431,9 +478,17 @@ def run_ours(args, log):
     sim._L.rp_enable_gpu(sim._h, local)
     if args.host_loop:
         sim._L.rp_set_device_loop(sim._h, 0)
+    jkr = None
+    if wl["normal"] == "jkr":
+        solver = args.jkr_solver or "learned"
+        jkr = {"solver": solver}
+        if solver == "learned":
+            jkr["training"] = sim.train_jkr_network(seed=1)
+        sim.set_jkr_solver(solver)
     sim.steps(args.warmup)
     torch.cuda.synchronize()
     s0 = sim.stats()
+    c0 = sim.jkr_counters() if jkr else None
     clocks = ClockSampler(local)
     barrier(dist)
     torch.cuda.synchronize()
@@ -445,6 +500,14 @@ def run_ours(args, log):
     barrier(dist)
     ck = clocks.stop()
     s1 = sim.stats()
+    if jkr:
+        c1 = sim.jkr_counters()
+        d = {k: (c1[k] - c0[k]) / args.steps for k in c1}
+        ev = d["accepted"] + d["zero"] + d["fallback"]
+        jkr["per_step"] = d
+        if ev > 0:
+            jkr["fraction"] = {"converging": d["accepted"] / ev, "certified_zero": d["zero"] / ev,
+                               "reference_newton": d["fallback"] / ev}
     dev_ms = s1["device_ms"] - s0["device_ms"]
     n_now = s1["particles"]
     t_max = allreduce_max(dist, dev_ms)
@@ -506,6 +569,8 @@ def run_ours(args, log):
         "gpu_launches": int(launches), "clocks": ck,
         "stats": {k: s1[k] for k in ("neighbor_rebuilds", "max_neighbors", "neighbor_capacity", "removed")},
     }
+    if jkr:
+        line["config"]["jkr"] = jkr
     print(json.dumps(line), flush=True)
     barrier(dist)
     return 0
@@ -517,12 +582,15 @@ def main():
     ap.add_argument("--steps", type=int, default=500)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["hopper", "box"], default="hopper")
+    ap.add_argument("--workload", choices=["hopper", "box", "adhesive"], default="hopper")
+    ap.add_argument("--jkr-solver", choices=["newton", "learned", "certified"], default=None,
+                    help="JKR solver of the adhesive workload (default learned)")
     ap.add_argument("--mode", choices=["parity", "physical"], default="parity")
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
-    ap.add_argument("--particles", type=int, default=1_048_576, help="hopper workload size")
+    ap.add_argument("--particles", type=int, default=None,
+                    help="workload size (hopper 1,048,576, adhesive 4,194,304 by default)")
     ap.add_argument("--state-in", default=None, help="relaxed positions (.npz) instead of relaxing")
     ap.add_argument("--state-out", default=None, help="save the relaxed positions (.npz)")
     ap.add_argument("--host-loop", action="store_true", help="host-issued kernels instead of the device loop")

@@ -197,6 +197,81 @@ int rp_debug_contact_pairs(rp_sim* sim, int64_t* pi, int64_t* pj, int32_t* visit
 int rp_debug_reference_grid(rp_sim* sim, double h, int64_t* cell_of, int64_t* order, size_t* n_order,
                             int32_t dims[3]);
 
+/* --- learned JKR contact radius (no counterpart in the reference; replaces
+ * the per-contact Newton iteration of src/physics.rs:164-191 for particle
+ * pairs of the JKR model)
+ *
+ * Solvers (rp_set_jkr_solver):
+ *   RP_JKR_NEWTON  the reference's Newton iteration (default)
+ *   RP_JKR_LEARNED exact certificates decide pairs where the reference returns
+ *                  zero or provably converges; the latter take a/R* from a
+ *                  4-64-64-64-1 network (BF16 weights, FP32 accumulation, on
+ *                  the tensor cores), two FP32 Newton steps, an FP64 residual
+ *                  check (relative residual > 1e-6 -> the reference's Newton)
+ *                  and one FP64 correction. Needs a network (rp_jkr_train or
+ *                  rp_jkr_set_network).
+ *   RP_JKR_CERTIFIED the same certificates and checks without the network
+ *                  (FP32 Newton from the reference's start): the method
+ *                  without its learned part. */
+#define RP_JKR_NEWTON 0
+#define RP_JKR_LEARNED 1
+#define RP_JKR_CERTIFIED 2
+#define RP_MLP_PARAMS 8705 /* FP32 parameters: W1[64][4] b1 W2[64][64] b2 W3[64][64] b3 W4[64] b4 */
+
+typedef struct rp_jkr_train_options {
+  double rs_min, rs_max;  /* effective radius range; 0 = r_min/2 .. r_max/2 of the particles */
+  double es_scale;        /* E* sampled log-uniform from E* over s to E* times s; 0 = 1.25 */
+  double gamma_scale;     /* surface energy likewise; 0 = 1.25 */
+  double x_min, x_max;    /* overlap / R* range; both 0 = [-0.1, 0.2] */
+  uint64_t seed;          /* 0 = 1 */
+  uint64_t samples;       /* power of two; 0 = 1,048,576 */
+  int32_t epochs;         /* 0 = 24 */
+  int32_t batch;          /* multiple of 64; 0 = 8192 */
+  float lr0, lr1;         /* cosine schedule; 0 = 3e-3 .. 2e-5 */
+  int32_t qat_from_epoch; /* quantisation-aware from this epoch; 0 = epochs / 2, < 0 = from the start */
+} rp_jkr_train_options;
+
+typedef struct rp_jkr_train_report {
+  double final_loss;    /* last mini-batch loss (normalised target) */
+  double val_rms;       /* held-out error of the BF16 network in t = ln(a/R*) - ln sqrt(max(x,0)+c^(2/3)) */
+  double val_max;
+  double train_ms;      /* wall time of sample generation + training */
+  uint64_t samples, valid_samples, steps;
+} rp_jkr_train_report;
+
+/* Generates samples with the reference's Newton solver on the GPU, trains the
+ * network there with the project's forward/backward/Adam kernels, and installs
+ * it in the simulation. options/report may be NULL. Material and radii must
+ * be set before the call. */
+int rp_jkr_train(rp_sim* sim, const rp_jkr_train_options* options, rp_jkr_train_report* report);
+int rp_set_jkr_solver(rp_sim* sim, int solver);
+/* The installed network: params[RP_MLP_PARAMS], norm[10] (feature mean[4],
+ * 1/std[4], target mean, std), domain[8] (raw-feature min[4], max[4]). */
+int rp_jkr_get_network(rp_sim* sim, float* params, float* norm, float* domain);
+int rp_jkr_set_network(rp_sim* sim, const float* params, const float* norm, const float* domain);
+/* Pair evaluations since the last upload: [0] accepted by the certified solver,
+ * [1] certified zero, [2] reference-Newton fallbacks, [3] network rows used,
+ * [4] FP32 Newton steps, [5] pairs decided by the closed-form walk. */
+int rp_jkr_counters(rp_sim* sim, uint64_t out[6]);
+
+/* Building blocks of the learned solver, on the current CUDA device (host
+ * buffers in and out). Features and targets are normalised. */
+/* Loss sum_s w_s (y_s - t_s)^2 / n and its gradient for n samples (n a power
+ * of two, >= 64); qat = 1 evaluates the forward pass as inference does (BF16
+ * weights and layer inputs, tanh.approx) with straight-through gradients. */
+int rp_mlp_loss_grad(const float* params, const float* features, const float* targets, const float* weights, size_t n,
+                     int qat, float* grad, double* loss);
+/* Tensor-core inference (BF16 weights rounded to nearest even) on n rows. */
+int rp_mlp_infer(const float* params, const float* features, size_t n, float* out);
+/* Training samples: domain = {rs_lo, rs_hi, E*_lo, E*_hi, gamma_lo, gamma_hi,
+ * x_lo, x_hi}; writes raw features (4n), target t (n), weight (n, 1 where the
+ * network applies), the reference Newton's a (n, may be NULL) and its loop
+ * count (n, may be NULL; negative where the pair is not network-eligible),
+ * and the FP64 inputs (overlap, R*, E*, gamma) of each sample (4n, may be
+ * NULL). */
+int rp_jkr_samples(const double domain[8], uint64_t seed, size_t n, float* features, float* targets, float* weights,
+                   double* a_ref, int32_t* iters, double* inputs);
+
 /* --- allocation-free cell sort (no counterpart in the reference)
  * For callers that cannot call cudaMalloc: code issuing work inside a CUDA
  * stream capture, engines whose pool allocator owns all device memory, and

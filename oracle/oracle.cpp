@@ -160,15 +160,17 @@ V3<T> hertz_elastic(T overlap, V3<T> n, T es, T rs) {
   tl_terms += std::fabs((double)f);
   return f * n;
 }
-// src/physics.rs:132-219
+// The Newton iteration for the JKR contact radius, src/physics.rs:164-191;
+// `iters` receives the number of loop bodies run.
 template <typename T>
-V3<T> jkr(T overlap, V3<T> n, T es, T rs, T gamma) {
-  if (gamma <= T(0)) return hertz_elastic(overlap, n, es, rs);
+T jkr_radius(T overlap, T es, T rs, T gamma, int* iters) {
   const T eight_pi = T(8) * pi<T>();
   T c_val = eight_pi * gamma / es;
   T sqrt_c = std::sqrt(c_val);
   T a = overlap > T(0) ? std::sqrt(rs * overlap) : rs * T(0.5);
-  for (int it = 0; it < 20; ++it) {
+  int it = 0;
+  while (it < 20) {
+    ++it;
     if (a <= T(0)) a = T(1e-9);
     T ts = std::sqrt(c_val * a);
     T f_val = a * a / rs - ts - overlap;
@@ -180,6 +182,16 @@ V3<T> jkr(T overlap, V3<T> n, T es, T rs, T gamma) {
     a = a - step;
     if (std::fabs(step) < T(1e-6) * rs) break;
   }
+  if (iters) *iters = it;
+  return a;
+}
+// src/physics.rs:132-219
+template <typename T>
+V3<T> jkr(T overlap, V3<T> n, T es, T rs, T gamma) {
+  if (gamma <= T(0)) return hertz_elastic(overlap, n, es, rs);
+  const T eight_pi = T(8) * pi<T>();
+  T c_val = eight_pi * gamma / es;
+  T a = jkr_radius(overlap, es, rs, gamma, (int*)nullptr);
   T ts = std::sqrt(c_val * a);
   T f_val = a * a / rs - ts - overlap;
   if (std::fabs(f_val) > T(1e-3) * rs) return V3<T>();
@@ -951,5 +963,9 @@ int orc_triangle_query(int prec, const double* v9, const double* n3, const doubl
 // Scalar force-law probes (prec 64), for unit tests of the laws.
 double orc_jkr_force(double overlap, double es, double rs, double gamma) {
   return jkr<double>(overlap, V3<double>(1, 0, 0), es, rs, gamma).x;
+}
+// The contact radius the reference's Newton loop ends on, and its loop count.
+double orc_jkr_radius(double overlap, double es, double rs, double gamma, int* iters) {
+  return jkr_radius<double>(overlap, es, rs, gamma, iters);
 }
 }

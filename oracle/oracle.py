@@ -82,6 +82,7 @@ def lib():
             "orc_pairs": (None, [vp, lp, lp]),
             "orc_triangle_query": (i, [i, dp, dp, dp, d, dp, dp]),
             "orc_jkr_force": (d, [d, d, d, d]),
+            "orc_jkr_radius": (d, [d, d, d, d, ip]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -342,3 +343,15 @@ def triangle_query(v9, n3, c, r, prec=64):
     nrm = np.zeros(3)
     hit = lib().orc_triangle_query(prec, _dp(v9), _dp(n3), _dp(c), float(r), ctypes.byref(pen), _dp(nrm))
     return (pen.value, nrm) if hit else None
+
+
+def jkr_force(overlap, es, rs, gamma):
+    """Normal force magnitude of the reference's JKR law in FP64 (src/physics.rs:132-219)."""
+    return float(lib().orc_jkr_force(float(overlap), float(es), float(rs), float(gamma)))
+
+
+def jkr_radius(overlap, es, rs, gamma):
+    """(a, loop bodies run) of the reference's Newton iteration in FP64 (src/physics.rs:164-191)."""
+    it = ctypes.c_int()
+    a = lib().orc_jkr_radius(float(overlap), float(es), float(rs), float(gamma), ctypes.byref(it))
+    return float(a), int(it.value)

@@ -277,6 +277,52 @@ class Simulation:
                                               order.ctypes.data_as(_lib._i64p), ctypes.byref(no), dims))
         return tuple(dims), cell[:n], order[:no.value]
 
+    # ---- learned JKR contact radius ---------------------------------------
+    def train_jkr_network(self, **options):
+        """Generate Newton-solved samples and train the JKR network on the GPU.
+
+        Keyword options are the fields of ``rp_jkr_train_options`` (rs_min,
+        rs_max, es_scale, gamma_scale, x_min, x_max, seed, samples, epochs,
+        batch, lr0, lr1, qat_from_epoch); returns the training report as a dict.
+        """
+        o = _lib.RpJkrTrainOptions()
+        for k, v in options.items():
+            if k not in dict(_lib.RpJkrTrainOptions._fields_):
+                raise TypeError(f"unknown option {k!r}")
+            setattr(o, k, v)
+        r = _lib.RpJkrTrainReport()
+        check(self._L.rp_jkr_train(self._h, ctypes.byref(o), ctypes.byref(r)))
+        return {k: getattr(r, k) for k, _ in _lib.RpJkrTrainReport._fields_}
+
+    def set_jkr_solver(self, solver):
+        """'newton' (the reference's iteration), 'learned' or 'certified' (no network)."""
+        s = {"newton": _lib.RP_JKR_NEWTON, "learned": _lib.RP_JKR_LEARNED,
+             "certified": _lib.RP_JKR_CERTIFIED}.get(solver, solver)
+        check(self._L.rp_set_jkr_solver(self._h, int(s)))
+
+    def get_jkr_network(self):
+        """(params[8705], norm[10], domain[8]) of the installed network, float32."""
+        p = np.zeros(_lib.RP_MLP_PARAMS, np.float32)
+        nm = np.zeros(10, np.float32)
+        dm = np.zeros(8, np.float32)
+        check(self._L.rp_jkr_get_network(self._h, p.ctypes.data_as(_lib._fp), nm.ctypes.data_as(_lib._fp),
+                                         dm.ctypes.data_as(_lib._fp)))
+        return p, nm, dm
+
+    def set_jkr_network(self, params, norm, domain):
+        p = np.ascontiguousarray(params, np.float32)
+        nm = np.ascontiguousarray(norm, np.float32)
+        dm = np.ascontiguousarray(domain, np.float32)
+        if p.size != _lib.RP_MLP_PARAMS or nm.size != 10 or dm.size != 8:
+            raise ValueError("network needs 8705 parameters, 10 normalisation and 8 domain values")
+        check(self._L.rp_jkr_set_network(self._h, p.ctypes.data_as(_lib._fp), nm.ctypes.data_as(_lib._fp),
+                                         dm.ctypes.data_as(_lib._fp)))
+
+    def jkr_counters(self):
+        out = (ctypes.c_uint64 * 6)()
+        check(self._L.rp_jkr_counters(self._h, out))
+        return dict(zip(("accepted", "zero", "fallback", "network_rows", "fp32_newton_steps", "walk"), list(out)))
+
     def _warn(self):
         """The reference prints a warning on every step with an overlap above
         20 % of a radius (src/simulation.rs:528-530); here once per call."""

@@ -64,6 +64,42 @@ class RpStats(ctypes.Structure):
     ]
 
 
+RP_JKR_NEWTON, RP_JKR_LEARNED, RP_JKR_CERTIFIED = 0, 1, 2
+RP_MLP_PARAMS = 8705
+_fp = ctypes.POINTER(ctypes.c_float)
+_u64p = ctypes.POINTER(ctypes.c_uint64)
+
+
+class RpJkrTrainOptions(ctypes.Structure):
+    _fields_ = [
+        ("rs_min", ctypes.c_double),
+        ("rs_max", ctypes.c_double),
+        ("es_scale", ctypes.c_double),
+        ("gamma_scale", ctypes.c_double),
+        ("x_min", ctypes.c_double),
+        ("x_max", ctypes.c_double),
+        ("seed", ctypes.c_uint64),
+        ("samples", ctypes.c_uint64),
+        ("epochs", ctypes.c_int32),
+        ("batch", ctypes.c_int32),
+        ("lr0", ctypes.c_float),
+        ("lr1", ctypes.c_float),
+        ("qat_from_epoch", ctypes.c_int32),
+    ]
+
+
+class RpJkrTrainReport(ctypes.Structure):
+    _fields_ = [
+        ("final_loss", ctypes.c_double),
+        ("val_rms", ctypes.c_double),
+        ("val_max", ctypes.c_double),
+        ("train_ms", ctypes.c_double),
+        ("samples", ctypes.c_uint64),
+        ("valid_samples", ctypes.c_uint64),
+        ("steps", ctypes.c_uint64),
+    ]
+
+
 # name -> (restype, argtypes); the list of exported entry points of rp.h
 SIGNATURES = {
     "rp_create": (ctypes.c_void_p, [ctypes.c_double, _dp, _dp, ctypes.c_size_t]),
@@ -113,6 +149,16 @@ SIGNATURES = {
                                                ctypes.POINTER(ctypes.c_size_t), _i32p]),
     "rp_cell_sort_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_size_t, _dp, ctypes.c_double, _i32p,
                                             ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "rp_jkr_train": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(RpJkrTrainOptions),
+                                    ctypes.POINTER(RpJkrTrainReport)]),
+    "rp_set_jkr_solver": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "rp_jkr_get_network": (ctypes.c_int, [ctypes.c_void_p, _fp, _fp, _fp]),
+    "rp_jkr_set_network": (ctypes.c_int, [ctypes.c_void_p, _fp, _fp, _fp]),
+    "rp_jkr_counters": (ctypes.c_int, [ctypes.c_void_p, _u64p]),
+    "rp_mlp_loss_grad": (ctypes.c_int, [_fp, _fp, _fp, _fp, ctypes.c_size_t, ctypes.c_int, _fp,
+                                        ctypes.POINTER(ctypes.c_double)]),
+    "rp_mlp_infer": (ctypes.c_int, [_fp, _fp, ctypes.c_size_t, _fp]),
+    "rp_jkr_samples": (ctypes.c_int, [_dp, ctypes.c_uint64, ctypes.c_size_t, _fp, _fp, _fp, _dp, _i32p, _dp]),
 }
 
 _lib = None

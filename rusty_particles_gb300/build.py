@@ -20,10 +20,10 @@ LIB = os.path.join(BUILD, "librp.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2", "--expt-relaxed-constexpr",
           "-I", CSRC]
-# Per-file extra flags: the step kernels must not fuse multiply-adds (their
-# rounding has to match the oracle's).
-EXTRA = {"k_step.cu": ["-fmad=false"]}
-SOURCES = ["k_broadphase.cu", "k_step.cu", "engine.cu", "rp_api.cu", "k_noalloc.cu"]
+# Per-file extra flags: the step kernels and the JKR sample generator must not
+# fuse multiply-adds (their rounding has to match the oracle's).
+EXTRA = {"k_step.cu": ["-fmad=false"], "k_mlp.cu": ["-fmad=false"]}
+SOURCES = ["k_broadphase.cu", "k_step.cu", "engine.cu", "rp_api.cu", "k_noalloc.cu", "k_mlp.cu"]
 
 
 def nvcc() -> str:

@@ -103,6 +103,8 @@ void Engine::free_device() {
   dfree(crec_); dfree(clist_); dfree(cres_); dfree(ccnt_); dfree(ncomp_); dfree(coff_); dfree(poff_);
   dfree(ctot_); dfree(cpart_);
   dfree(tri_d_); dfree(tstart_d_); dfree(titems_d_);
+  dfree(mlp_d_); dfree(jq_); dfree(jguess_); dfree(nnet_); dfree(noff_);
+  jq_alloc_ = 0;
   dfree(ctrl_);
   if (ctrl_h_) cudaFreeHost(ctrl_h_);
   ctrl_h_ = nullptr;
@@ -224,7 +226,8 @@ int Engine::alloc_slots(size_t n) {
   TRY(dalloc(&rb_.part, scan_parts_needed(std::max<uint32_t>(hn, (uint32_t)na)) + 16));
   TRY(dalloc(&dbgF_, 3 * na)); TRY(dalloc(&dbgT_, 3 * na));
   TRY(dalloc(&ccnt_, na)); TRY(dalloc(&ncomp_, na)); TRY(dalloc(&coff_, na)); TRY(dalloc(&poff_, na));
-  TRY(dalloc(&ctot_, 2)); TRY(dalloc(&cpart_, scan_parts_needed((uint32_t)na) + 16));
+  TRY(dalloc(&nnet_, na)); TRY(dalloc(&noff_, na));
+  TRY(dalloc(&ctot_, 3)); TRY(dalloc(&cpart_, scan_parts_needed((uint32_t)na) + 16));
   n_alloc_ = na;
   // lists must be re-allocated for the new slot count
   for (int b = 0; b < 2; ++b) {
@@ -278,6 +281,34 @@ int Engine::alloc_lists(int cap, bool keep_current) {
   cap_ = cap;
   graph_dirty_ = true;
   refresh_list_ptrs();
+  TRY(ensure_jkr_buffers());
+  return RP_OK;
+}
+
+// Network queue and per-record predictions (one entry per possible
+// evaluating record) and the device copy of the network, for the learned
+// JKR solver only.
+int Engine::ensure_jkr_buffers() {
+  if (jkr_solver != RP_JKR_LEARNED || !gpu_ || !jkr_have_net_) {
+    P_.mlp = nullptr;
+    return RP_OK;
+  }
+  const size_t need = std::max<size_t>(n_alloc_ * (size_t)std::max(cap_, 1), 1);
+  if (jq_alloc_ < need) {
+    TRY(dalloc(&jq_, need));
+    TRY(dalloc(&jguess_, need));
+    jq_alloc_ = need;
+    graph_dirty_ = true;
+  }
+  if (!mlp_d_) {
+    TRY(dalloc(&mlp_d_, 1));
+    MlpInfer h;
+    mlp_make_infer(jkr_params_.data(), jkr_norm_, &h);
+    CK(cudaMemcpy(mlp_d_, &h, sizeof(MlpInfer), cudaMemcpyHostToDevice));
+  }
+  P_.mlp = mlp_d_;
+  P_.jq = jq_;
+  P_.jguess = jguess_;
   return RP_OK;
 }
 
@@ -293,6 +324,8 @@ void Engine::refresh_list_ptrs() {
   P_.ncomp = ncomp_;
   P_.coff = coff_;
   P_.poff = poff_;
+  P_.nnet = nnet_;
+  P_.noff = noff_;
   P_.ctot = ctot_;
   P_.cpart = cpart_;
 }
@@ -329,6 +362,7 @@ int Engine::build_params() {
   }
   // reference grid: dims = ceil(size / h) + 1 (src/grid.rs:13)
   P.href = href;
+  P.inv_href = 1.0 / href;
   for (int k = 0; k < 3; ++k) {
     double q = std::ceil(P.bsize[k] / href);
     if (!(q >= 0.0) || q > (double)((1 << 20) - 4)) {
@@ -392,7 +426,16 @@ int Engine::build_params() {
   P.dbgT = dbgT_;
   P.ctrl = ctrl_;
   P.force_path = force_path;
+  // JKR of particle pairs: C = 8 pi gamma / E* as src/physics.rs:165 forms it
+  P.jkr_solver = jkr_solver;
+  P.jkr_C = (8.0 * kPiH) * P.gamma_pp / P.es_pp;
+  P.jkr_Cf = (float)P.jkr_C;
+  for (int k = 0; k < 4; ++k) {
+    P.jdom_lo[k] = jkr_dom_[k];
+    P.jdom_hi[k] = jkr_dom_[4 + k];
+  }
   refresh_list_ptrs();
+  TRY(ensure_jkr_buffers());
   return RP_OK;
 }
 
@@ -439,9 +482,24 @@ int Engine::build_triangle_grid(double rmax) {
       double cx = r.e0[1] * r.e1[2] - r.e0[2] * r.e1[1], cy = r.e0[2] * r.e1[0] - r.e0[0] * r.e1[2],
              cz = r.e0[0] * r.e1[1] - r.e0[1] * r.e1[0];
       double l = std::sqrt(cx * cx + cy * cy + cz * cz);
+      for (int e = 0; e < 3; ++e) r.edge[e] = make_float4(0.f, 0.f, 0.f, 1e30f);  // never rejects
       if (l > 0.0 && std::isfinite(l)) {
         cx /= l; cy /= l; cz /= l;
         r.plane = make_float4((float)cx, (float)cy, (float)cz, (float)(cx * v0[0] + cy * v0[1] + cz * v0[2]));
+        // in-plane unit normals of the edges, pointing away from the triangle
+        const double* vv[3] = {v0, v1, v2};
+        for (int e = 0; e < 3; ++e) {
+          const double *p = vv[e], *q2 = vv[(e + 1) % 3], *o = vv[(e + 2) % 3];
+          const double d[3] = {q2[0] - p[0], q2[1] - p[1], q2[2] - p[2]};
+          double m[3] = {d[1] * cz - d[2] * cy, d[2] * cx - d[0] * cz, d[0] * cy - d[1] * cx};
+          const double ml = std::sqrt(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]);
+          if (!(ml > 0.0) || !std::isfinite(ml)) continue;
+          for (int k = 0; k < 3; ++k) m[k] /= ml;
+          if (m[0] * (o[0] - p[0]) + m[1] * (o[1] - p[1]) + m[2] * (o[2] - p[2]) > 0.0)
+            for (int k = 0; k < 3; ++k) m[k] = -m[k];
+          r.edge[e] = make_float4((float)m[0], (float)m[1], (float)m[2],
+                                  (float)(m[0] * p[0] + m[1] * p[1] + m[2] * p[2]));
+        }
       } else {
         r.plane = make_float4(0.f, 0.f, 0.f, 0.f);
       }
@@ -557,7 +615,9 @@ int Engine::upload() {
     a8[4][i] = D4{p.tau[0], p.tau[1], p.tau[2], 0.0};
     a8[5][i] = D4{p.xres[0], p.xres[1], p.xres[2], 0.0};
     a8[6][i] = D4{p.vres[0], p.vres[1], p.vres[2], 0.0};
-    a8[7][i] = D4{p.wres[0], p.wres[1], p.wres[2], 0.0};
+    // .w carries 1 / I = 1 / (0.4 m r^2) (constant per particle; the same
+    // correctly rounded division the step would do)
+    a8[7][i] = D4{p.wres[0], p.wres[1], p.wres[2], 1.0 / (0.4 * p.m * p.r * p.r)};
     flags[i] = p.fixed ? PF_FIXED : 0u;
     tags[i] = p.tag;
   }
@@ -717,8 +777,8 @@ int Engine::build_graph() {
   cudaGraphConditionalHandle hif;
   CK(cudaGraphConditionalHandleCreate(&hif, body, 0, cudaGraphCondAssignDefault));
   CK(cudaStreamBeginCaptureToGraph(cap_stream_, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
-  launch_first_half(P_, cap_stream_);
-  launch_rebuild_condition(P_, hif, cap_stream_);
+  int sk = launch_first_half(P_, cap_stream_);
+  sk += launch_rebuild_condition(P_, hif, cap_stream_);
   cudaStreamCaptureStatus st;
   cudaGraph_t cg = nullptr;
   const cudaGraphNode_t* deps = nullptr;
@@ -737,8 +797,9 @@ int Engine::build_graph() {
   chain_kernels_ = launch_rebuild(P_, rb_, cap_stream2_);
   cudaGraph_t t2 = nullptr;
   CK(cudaStreamEndCapture(cap_stream2_, &t2));
-  launch_force(P_, cap_stream_);
-  launch_end_step_loop(P_, hloop, cap_stream_);
+  sk += launch_force(P_, cap_stream_);
+  sk += launch_end_step_loop(P_, hloop, cap_stream_);
+  step_kernels_ = sk;
   cudaGraph_t t1 = nullptr;
   CK(cudaStreamEndCapture(cap_stream_, &t1));
   CK(cudaGraphInstantiate(&graph_exec_, g, 0));
@@ -771,7 +832,8 @@ int Engine::launch_steps_graph(uint64_t n) {
     cudaEventElapsedTime(&ms, ev0_, ev1_);
     ms_total_ += ms;
     TRY(recover_halt());
-    launches_ += 4 * (ctrl_h_->steps_done - before) + (uint64_t)chain_kernels_ * (ctrl_h_->rebuilds - rb_before);
+    launches_ += (uint64_t)step_kernels_ * (ctrl_h_->steps_done - before) +
+                 (uint64_t)chain_kernels_ * (ctrl_h_->rebuilds - rb_before);
     TRY(finish_step_accounting());
     const uint64_t done = last_.steps_done - before;
     if (done == 0) {
@@ -1035,6 +1097,7 @@ int Engine::debug_reference_grid(double h, int64_t* cell_of, int64_t* order, siz
   const size_t n = hp_.size();
   StepParams P = P_;
   P.href = h;
+  P.inv_href = 1.0 / h;
   uint64_t ncells = 1;
   for (int k = 0; k < 3; ++k) {
     P.bmin[k] = bmin[k];
@@ -1079,6 +1142,122 @@ int Engine::debug_reference_grid(double h, int64_t* cell_of, int64_t* order, siz
     if (sk[k] < ncells) order[m++] = (int64_t)sv[k];
   *n_order = m;
   // the device upload used the sort buffers: the next step rebuilds anyway
+  return RP_OK;
+}
+
+// ------------------------------------------------------------ learned JKR
+// Trains on the particle-pair domain of this simulation: R* between half the
+// smallest and half the largest radius (or the given range), E* and gamma of
+// the particle material scaled both ways, overlap/R* in [x_min, x_max].
+int Engine::jkr_train(const rp_jkr_train_options* o, rp_jkr_train_report* rep) {
+  rp_jkr_train_options d;
+  std::memset(&d, 0, sizeof(d));
+  if (o) d = *o;
+  TRY(ensure_gpu());
+  double rmin = 0.0, rmax = 0.0;
+  if (!host_valid_) TRY(download());
+  for (size_t i = 0; i < hp_.size(); ++i) {
+    rmin = i == 0 ? hp_[i].r : std::min(rmin, hp_[i].r);
+    rmax = std::max(rmax, hp_[i].r);
+  }
+  JkrTrainConfig cfg;
+  std::memset(&cfg, 0, sizeof(cfg));
+  cfg.dom.rs_lo = d.rs_min > 0.0 ? d.rs_min : 0.5 * rmin;
+  cfg.dom.rs_hi = d.rs_max > 0.0 ? d.rs_max : 0.5 * rmax;
+  if (!(cfg.dom.rs_lo > 0.0) || !(cfg.dom.rs_hi >= cfg.dom.rs_lo)) {
+    set_error("JKR training needs particles (or rs_min/rs_max) to fix the effective-radius range");
+    return RP_E_INVALID_ARG;
+  }
+  if (cfg.dom.rs_hi <= cfg.dom.rs_lo) cfg.dom.rs_hi = cfg.dom.rs_lo * (1.0 + 1e-6);
+  const double es = eff_youngs(pm.E, pm.nu, pm.E, pm.nu);
+  const double gamma = (pm.gamma + pm.gamma) * 0.5;
+  if (!(gamma > 0.0) || !(es > 0.0)) {
+    set_error("JKR training needs a positive surface energy and Young's modulus");
+    return RP_E_INVALID_ARG;
+  }
+  const double se = d.es_scale > 1.0 ? d.es_scale : 1.25, sg = d.gamma_scale > 1.0 ? d.gamma_scale : 1.25;
+  cfg.dom.es_lo = es / se;
+  cfg.dom.es_hi = es * se;
+  cfg.dom.gamma_lo = gamma / sg;
+  cfg.dom.gamma_hi = gamma * sg;
+  cfg.dom.x_lo = (d.x_min == 0.0 && d.x_max == 0.0) ? -0.1 : d.x_min;
+  cfg.dom.x_hi = (d.x_min == 0.0 && d.x_max == 0.0) ? 0.2 : d.x_max;
+  if (!(cfg.dom.x_hi > cfg.dom.x_lo)) {
+    set_error("x_max must exceed x_min");
+    return RP_E_INVALID_ARG;
+  }
+  cfg.seed = d.seed ? d.seed : 1;
+  cfg.n_samples = d.samples ? (size_t)d.samples : (size_t)1 << 20;
+  cfg.epochs = d.epochs > 0 ? d.epochs : 24;
+  cfg.batch = d.batch > 0 ? d.batch : 8192;
+  cfg.lr0 = d.lr0 > 0.f ? d.lr0 : 3e-3f;
+  cfg.lr1 = d.lr1 > 0.f ? d.lr1 : 2e-5f;
+  cfg.qat_from_epoch = d.qat_from_epoch > 0 ? d.qat_from_epoch : (d.qat_from_epoch < 0 ? 0 : cfg.epochs / 2);
+  cfg.n_val = 65536;
+  if ((cfg.n_samples & (cfg.n_samples - 1)) != 0 || cfg.n_samples < 1024 || cfg.batch % 64 != 0 ||
+      (size_t)cfg.batch > cfg.n_samples) {
+    set_error("samples must be a power of two >= 1024 and batch a multiple of 64 not above it");
+    return RP_E_INVALID_ARG;
+  }
+  JkrTrainResult* R = new (std::nothrow) JkrTrainResult;
+  if (!R) return RP_E_NOMEM;
+  const int rc = rp::jkr_train(cfg, R, stream_);
+  if (rc != 0) {
+    delete R;
+    set_error("JKR network training failed (code %d)", rc);
+    return RP_E_CUDA;
+  }
+  float dom[8];
+  for (int k = 0; k < 4; ++k) {
+    dom[k] = R->lo[k];
+    dom[4 + k] = R->hi[k];
+  }
+  const int r2 = jkr_set_network(R->params, R->norm, dom);
+  if (rep) {
+    rep->final_loss = R->final_loss;
+    rep->val_rms = R->val_rms;
+    rep->val_max = R->val_max;
+    rep->train_ms = R->train_ms;
+    rep->samples = cfg.n_samples;
+    rep->valid_samples = R->n_valid;
+    rep->steps = R->steps;
+  }
+  delete R;
+  return r2;
+}
+
+int Engine::jkr_set_network(const float* params, const float* norm, const float* domain) {
+  for (int k = 0; k < MLP_NPARAM; ++k)
+    if (!std::isfinite(params[k])) {
+      set_error("network parameter %d is not finite", k);
+      return RP_E_INVALID_ARG;
+    }
+  jkr_params_.assign(params, params + MLP_NPARAM);
+  std::memcpy(jkr_norm_, norm, sizeof(jkr_norm_));
+  std::memcpy(jkr_dom_, domain, sizeof(jkr_dom_));
+  jkr_have_net_ = true;
+  if (gpu_) dfree(mlp_d_);  // re-uploaded with the new weights
+  dev_valid_ = false;
+  return RP_OK;
+}
+
+int Engine::jkr_get_network(float* params, float* norm, float* domain) {
+  if (!jkr_have_net_) {
+    set_error("no JKR network installed");
+    return RP_E_INVALID_ARG;
+  }
+  if (params) std::memcpy(params, jkr_params_.data(), sizeof(float) * MLP_NPARAM);
+  if (norm) std::memcpy(norm, jkr_norm_, sizeof(jkr_norm_));
+  if (domain) std::memcpy(domain, jkr_dom_, sizeof(jkr_dom_));
+  return RP_OK;
+}
+
+int Engine::jkr_counters(uint64_t out[6]) {
+  for (int k = 0; k < 6; ++k) out[k] = 0;
+  if (!gpu_ || !dev_valid_) return RP_OK;
+  CK(cudaSetDevice(device_));
+  TRY(sync_ctrl());
+  for (int k = 0; k < 6; ++k) out[k] = ctrl_h_->jkr_count[k];
   return RP_OK;
 }
 

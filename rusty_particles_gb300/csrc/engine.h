@@ -11,6 +11,7 @@
 #include "../../include/rp.h"
 #include "rp_device.cuh"
 #include "rp_launch.h"
+#include "rp_mlp.cuh"
 
 namespace rp {
 
@@ -59,6 +60,13 @@ class Engine {
   int debug_pairs(int64_t* pi, int64_t* pj, int32_t* visits, size_t capacity, size_t* n);
   int debug_reference_grid(double h, int64_t* cell_of, int64_t* order, size_t* n_order, int32_t dims[3]);
   int write_vtk(const char* path);
+  // learned JKR (RP_JKR_*)
+  int jkr_solver = RP_JKR_NEWTON;
+  int jkr_train(const rp_jkr_train_options* o, rp_jkr_train_report* rep);
+  int jkr_set_network(const float* params, const float* norm, const float* domain);
+  int jkr_get_network(float* params, float* norm, float* domain);
+  bool jkr_has_network() const { return jkr_have_net_; }
+  int jkr_counters(uint64_t out[6]);
   void config_changed() { dev_valid_ = false; }  // forces a fresh upload before the next step
   void set_capacity(int c) {
     if (!host_valid_) download();
@@ -115,6 +123,18 @@ class Engine {
   double* cres_ = nullptr;
   void refresh_list_ptrs();
   double* ke_ = nullptr;
+  // learned JKR: installed network and its per-step queue
+  bool jkr_have_net_ = false;
+  std::vector<float> jkr_params_;
+  float jkr_norm_[10] = {};
+  float jkr_dom_[8] = {};
+  MlpInfer* mlp_d_ = nullptr;
+  uint2* jq_ = nullptr;
+  float* jguess_ = nullptr;
+  uint32_t *nnet_ = nullptr, *noff_ = nullptr;
+  size_t jq_alloc_ = 0;
+  int ensure_jkr_buffers();
+  int step_kernels_ = 4;  // kernels of one device-loop step outside the rebuild chain
   TriRec* tri_d_ = nullptr;
   uint32_t *tstart_d_ = nullptr, *titems_d_ = nullptr;
   StepParams P_ = {};

@@ -19,6 +19,7 @@
 
 #include "rp_device.cuh"
 #include "rp_launch.h"
+#include "rp_mlp.cuh"
 
 namespace rp {
 
@@ -108,6 +109,95 @@ __device__ __forceinline__ R jkr_mag(R overlap, R es, R rs, R gamma, bool* near 
   if (fm < f_pull) return R(0);
   return fm;
 }
+// JKR magnitude of a particle pair without the reference's Newton loop, or
+// JKR_FALLBACK when that loop must run (P.jkr_solver 1 or 2). The
+// certificates (rp_mlp.cuh) either prove the reference returns zero or that
+// its iteration converges to the root on the increasing branch; the root is
+// then found in FP32 (solver 1: two Newton steps from the network's `guess`;
+// solver 2: Newton from the reference's own start), accepted only when its
+// FP64 residual is <= 1e-6 of the terms, corrected by one FP64-accurate Newton
+// step, and turned into the reference's force 4 E* a^3/(3 R*) - sqrt(8 pi
+// gamma E* a^3) = E* a (4 a^2/(3 R*) - sqrt(C a)). The pull-off cut is decided
+// in FP64 and left to the reference's loop when within 1e-7 of the terms.
+__device__ __forceinline__ int jkr_learned(const StepParams& P, double overlap, double rs, float guess, double& fm,
+                                           uint32_t& iters) {
+  const float rsf = (float)rs;
+  const float x = (float)overlap / rsf;
+  const float c = P.jkr_Cf / rsf;
+  const float c23 = jkr_c23(c);
+  const int cls = jkr_certify(x, c, c23, overlap > 0.0);
+  if (cls == JKR_ZERO) {
+    fm = 0.0;
+    return JKR_ZERO;
+  }
+  if (cls == JKR_WALK) {
+    // the reference's halving walk, then its own tail (src/physics.rs:193-218),
+    // operation for operation in FP64
+    const double es = P.es_pp, gamma = P.gamma_pp;
+    const double eight_pi = 8.0 * kPi;
+    const double c_val = eight_pi * gamma / es;
+    double a = sqrt(rs * overlap);
+    const double lim = 1e-6 * rs;
+    for (int it = 0; it < 20; ++it) {
+      const double st = a * 0.5;
+      a = a - st;
+      if (st < lim) break;
+    }
+    const double ts = sqrt(c_val * a);
+    const double f_val = a * a / rs - ts - overlap;
+    fm = 0.0;
+    if (fabs(f_val) > 1e-3 * rs || a <= 0.0) return JKR_WALK;
+    const double a3 = a * a * a;
+    const double term1 = 4.0 * es * a3 / (3.0 * rs);
+    const double term2 = sqrt(eight_pi * gamma * es * a3);
+    const double fmv = term1 - term2;
+    const double f_pull = (-2.0 / 3.0) * kPi * gamma * rs;
+    fm = fmv < f_pull ? 0.0 : fmv;
+    return JKR_WALK;
+  }
+  if (cls != JKR_CONVERGES) return JKR_FALLBACK;
+  float u;
+  if (P.jkr_solver == 1) {
+    if (!(guess > 0.0f && guess < 1e30f)) return JKR_FALLBACK;
+    u = jkr_newton_f32(jkr_newton_f32(guess, x, c), x, c);
+    iters += 2;
+  } else {
+    u = overlap > 0.0 ? sqrtf(x) : 0.5f;
+    for (int k = 0; k < 40; ++k) {
+      const float un = jkr_newton_f32(u, x, c);
+      ++iters;
+      const bool done = fabsf(un - u) <= 1e-6f * un;
+      u = un;
+      if (done) break;
+    }
+  }
+  // FP64 residual of a = u R*: sqrt(C a) from the FP32 root plus one Newton
+  // step of the square root (error ~1e-14), no FP64 division
+  const double ud = (double)u;
+  const double Ca = P.jkr_C * (ud * rs);
+  const float s0 = sqrtf((float)Ca);
+  if (!(s0 > 0.0f)) return JKR_FALLBACK;
+  const double ts = (double)s0 + (Ca - (double)s0 * (double)s0) * (double)(0.5f / s0);
+  const double uu = ud * ud * rs;  // a^2 / R*
+  const double f = uu - ts - overlap;
+  if (!(fabs(f) <= 1e-6 * (uu + ts + fabs(overlap)))) return JKR_FALLBACK;
+  const float dg = 2.0f * u - 0.5f * (float)ts / ((float)ud * rsf);
+  if (!(dg > 0.0f)) return JKR_FALLBACK;
+  const float du = (float)f / (rsf * dg);
+  const double u1 = ud - (double)du;
+  const float q = du / u;
+  const double ts1 = ts * (1.0 - (double)(0.5f * q + 0.125f * q * q));
+  const double es = P.es_pp;
+  const double a1 = u1 * rs;
+  const double term1 = (4.0 / 3.0) * es * (u1 * u1 * u1) * (rs * rs);
+  const double term2 = es * a1 * ts1;
+  const double fmv = term1 - term2;
+  const double f_pull = (-2.0 / 3.0) * kPi * P.gamma_pp * rs;
+  if (fabs(fmv - f_pull) <= 1e-7 * (term1 + term2)) return JKR_FALLBACK;
+  fm = fmv < f_pull ? 0.0 : fmv;
+  return JKR_CONVERGES;
+}
+
 // src/physics.rs:234-325
 template <typename R>
 __device__ __forceinline__ R sjkr_mag(R overlap, R vn, R es, R rs, R gamma) {
@@ -187,10 +277,15 @@ __device__ __forceinline__ T3<R> spring_coulomb(R fn, T3<R> rv, T3<R> n, T3<R>& 
 // loading/unloading sign and detachment, JKR's cut-offs) or an sJKR
 // near-cancellation lies within FP32 rounding: the caller then evaluates the
 // pair in FP64, so both forms take the same branches.
+// With P.jkr_solver != 0 the JKR magnitude comes from jkr_learned (`guess` is
+// the network's a/R*, or negative / NaN for none; `tally` counts accepted /
+// zero / fallback and
+// FP32 Newton steps when not null).
 template <typename R, bool PHYS, bool HIST>
 __device__ __forceinline__ bool pair_contact(const StepParams& P, V d, double d2, double rsum, double ri, double rj,
                                              double mi, double mj, V vi, V vj, V wi, V wj, double* hist, size_t plane,
-                                             V& fc_out, V& tc_out, V& n_out, bool& excess) {
+                                             V& fc_out, V& tc_out, V& n_out, bool& excess, float guess = -1.0f,
+                                             uint32_t* tally = nullptr) {
   constexpr bool F32 = sizeof(R) == sizeof(float);
   R overlap;
   T3<R> n;
@@ -230,7 +325,19 @@ __device__ __forceinline__ bool pair_contact(const StepParams& P, V d, double d2
   const R rs = (rir * rjr) / (rir + rjr);
   const R ms = ((R)mi * (R)mj) / ((R)mi + (R)mj);
   R fmag;
-  if (F32 && P.nmodel == 3) {
+  int jkind = JKR_FALLBACK;
+  if (P.nmodel == 3 && P.jkr_solver != 0 && P.gamma_pp > 0.0) {
+    double fmd = 0.0;
+    uint32_t it = 0;
+    jkind = jkr_learned(P, (double)overlap, (double)rs, guess, fmd, it);
+    if (jkind != JKR_FALLBACK) fmag = (R)fmd;
+    if (tally) {
+      tally[jkind == JKR_CONVERGES ? 0 : (jkind == JKR_ZERO ? 1 : (jkind == JKR_WALK ? 5 : 2))] += 1;
+      tally[4] += it;
+    }
+  }
+  if (jkind != JKR_FALLBACK) {
+  } else if (F32 && P.nmodel == 3) {
     bool near = false;
     fmag = jkr_mag<R>(overlap, (R)P.es_pp, rs, (R)P.gamma_pp, &near);
     if (near) return false;
@@ -288,15 +395,15 @@ __device__ __forceinline__ bool pair_contact(const StepParams& P, V d, double d2
 
 // Second half of velocity Verlet for one particle (src/simulation.rs:541-561):
 // Kahan-compensated v += a dt/2 and omega += (tau/I) dt/2, I = 0.4 m r^2
-// (tau/I as tau * (1/I): one division instead of three; v and x are unchanged).
-__device__ __forceinline__ void second_half_kick(V& v, V& vres, V& w, V& wres, V a, V tau, double m, double r,
+// (tau/I as tau * (1/I), 1/I stored per particle in Bank::wres[k].w when the
+// state is uploaded; v and x are unchanged).
+__device__ __forceinline__ void second_half_kick(V& v, V& vres, V& w, V& wres, V a, V tau, double inv_inertia,
                                                  double dt) {
   V dv = (0.5 * a) * dt;
   V yv = dv - vres;
   V tv = v + yv;
   vres = (tv - v) - yv;
   v = tv;
-  double inv_inertia = 1.0 / (0.4 * m * r * r);
   V aa = tau * inv_inertia;
   V dw = (0.5 * aa) * dt;
   V yw = dw - wres;
@@ -331,13 +438,16 @@ __global__ void __launch_bounds__(256) k_first_half(StepParams P) {
     V x = xyz(xr), v = xyz(vm), w = xyz(wc);
     const bool moving = !(fl & PF_FIXED);
     V a = vmk(0.0, 0.0, 0.0), tau = a, vres = a, wres = a, xres = a;
+    double inv_inertia = 0.0;
     if (moving) {
       a = xyz(B.acc[k]);
       tau = xyz(B.tq[k]);
       vres = xyz(B.vres[k]);
-      wres = xyz(B.wres[k]);
+      const D4 wr4 = B.wres[k];
+      wres = xyz(wr4);
+      inv_inertia = wr4.w;
       xres = xyz(B.xres[k]);
-      if (FUSE) second_half_kick(v, vres, w, wres, a, tau, vm.w, xr.w, dt);
+      if (FUSE) second_half_kick(v, vres, w, wres, a, tau, inv_inertia, dt);
     }
     if (anyp) {
       if (P.periodic[0]) { if (x.x < P.bmin[0]) x.x = x.x + P.bsize[0]; else if (x.x >= P.bmax[0]) x.x = x.x - P.bsize[0]; }
@@ -368,7 +478,6 @@ __global__ void __launch_bounds__(256) k_first_half(StepParams P) {
       V tx = x + yx;
       xres = (tx - x) - yx;
       x = tx;
-      double inv_inertia = 1.0 / (0.4 * vm.w * xr.w * xr.w);
       V aa = tau * inv_inertia;
       V dw = (0.5 * aa) * dt;
       V yw = dw - wres;
@@ -378,7 +487,7 @@ __global__ void __launch_bounds__(256) k_first_half(StepParams P) {
       B.vm[k] = D4{v.x, v.y, v.z, vm.w};
       B.vres[k] = D4{vres.x, vres.y, vres.z, 0.0};
       B.xres[k] = D4{xres.x, xres.y, xres.z, 0.0};
-      B.wres[k] = D4{wres.x, wres.y, wres.z, 0.0};
+      B.wres[k] = D4{wres.x, wres.y, wres.z, inv_inertia};
       wc.x = w.x; wc.y = w.y; wc.z = w.z;
     }
     if (P.mode == 0) {
@@ -409,13 +518,14 @@ __global__ void __launch_bounds__(256) k_second_half(StepParams P) {
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < P.n; k += gridDim.x * blockDim.x) {
     uint32_t fl = B.flags[k];
     if (fl & (PF_DEAD | PF_FIXED)) continue;
-    D4 xr = B.xr[k], vm = B.vm[k], wc = B.wc[k];
-    V v = xyz(vm), w = xyz(wc), vres = xyz(B.vres[k]), wres = xyz(B.wres[k]);
-    second_half_kick(v, vres, w, wres, xyz(B.acc[k]), xyz(B.tq[k]), vm.w, xr.w, P.dt);
+    D4 vm = B.vm[k], wc = B.wc[k];
+    const D4 wr4 = B.wres[k];
+    V v = xyz(vm), w = xyz(wc), vres = xyz(B.vres[k]), wres = xyz(wr4);
+    second_half_kick(v, vres, w, wres, xyz(B.acc[k]), xyz(B.tq[k]), wr4.w, P.dt);
     B.vm[k] = D4{v.x, v.y, v.z, vm.w};
     B.wc[k] = D4{w.x, w.y, w.z, wc.w};
     B.vres[k] = D4{vres.x, vres.y, vres.z, 0.0};
-    B.wres[k] = D4{wres.x, wres.y, wres.z, 0.0};
+    B.wres[k] = D4{wres.x, wres.y, wres.z, wr4.w};
   }
 }
 
@@ -443,7 +553,20 @@ __device__ __forceinline__ void wall_forces(const StepParams& P, V xi, float4 xf
         // ~3e-7 (|x| + |n.v0|) + 1.1e-7 |x - v0|; the margin is larger
         const float4 pl = tr.plane;
         const float hd = fabsf(pl.x * xf.x + pl.y * xf.y + pl.z * xf.z - pl.w);
-        if (hd > rf + 1e-6f * (1.0f + xmag + fabsf(pl.w) + rf) + 2e-7f * (xmag + tr.bound.x)) continue;
+        const float mrg = 1e-6f * (1.0f + xmag + fabsf(pl.w) + rf) + 2e-7f * (xmag + tr.bound.x);
+        if (hd > rf + mrg) continue;
+        // the distance to the triangle is at least sqrt(hd^2 + s^2), s the
+        // largest outward in-plane distance to an edge line (each with the
+        // plane test's rounding margin; |m.v| <= sqrt(3) bound)
+        {
+          const float4 g0 = tr.edge[0], g1 = tr.edge[1], g2 = tr.edge[2];
+          const float s = fmaxf(fmaxf(g0.x * xf.x + g0.y * xf.y + g0.z * xf.z - g0.w,
+                                      g1.x * xf.x + g1.y * xf.y + g1.z * xf.z - g1.w),
+                                g2.x * xf.x + g2.y * xf.y + g2.z * xf.z - g2.w);
+          const float me = mrg + 4e-7f * tr.bound.x;
+          const float hl = fmaxf(hd - mrg, 0.0f), sl = fmaxf(s - me, 0.0f);
+          if (hl * hl + sl * sl > rf * rf * (1.0f + 1e-6f)) continue;
+        }
         // closest point, src/mesh.rs:45-117 (same regions and clamps)
         const V v0 = vmk(tr.v0[0] - xi.x, tr.v0[1] - xi.y, tr.v0[2] - xi.z);
         const V e0 = vmk(tr.e0[0], tr.e0[1], tr.e0[2]), e1 = vmk(tr.e1[0], tr.e1[1], tr.e1[2]);
@@ -639,6 +762,58 @@ __device__ __forceinline__ V mic(const StepParams& P, V d) {
   return d;
 }
 
+// Whether a JKR pair goes to the network queue: jkr_learned's certificate on
+// the FP32 position mirror, its xi thresholds widened by the mirror's
+// rounding (~2.4e-7 of the coordinates). A queued pair the exact test rejects
+// only wastes a network row; a converging pair without a row falls back to the
+// reference's Newton.
+__device__ __forceinline__ bool jkr_net_hint(const StepParams& P, float4 xif, float4 xjf) {
+  float fx = xif.x - xjf.x, fy = xif.y - xjf.y, fz = xif.z - xjf.z;
+  if (P.periodic[0]) { const float L = (float)P.bsize[0]; if (fx > 0.5f * L) fx -= L; else if (fx < -0.5f * L) fx += L; }
+  if (P.periodic[1]) { const float L = (float)P.bsize[1]; if (fy > 0.5f * L) fy -= L; else if (fy < -0.5f * L) fy += L; }
+  if (P.periodic[2]) { const float L = (float)P.bsize[2]; if (fz > 0.5f * L) fz -= L; else if (fz < -0.5f * L) fz += L; }
+  const float rsum = xif.w + xjf.w;
+  const float rs = xif.w * xjf.w / rsum;
+  const float c = P.jkr_Cf / rs;
+  if (!(c >= kJkrCMin && c <= kJkrCMax)) return false;
+  const float c23 = jkr_c23(c);
+  const float x = (rsum - sqrtf(fx * fx + fy * fy + fz * fz)) / rs;
+  const float X = fmaxf(fmaxf(fmaxf(fabsf(xif.x), fabsf(xif.y)), fabsf(xif.z)),
+                        fmaxf(fmaxf(fabsf(xjf.x), fabsf(xjf.y)), fabsf(xjf.z)));
+  const float m = 0.02f + 2.4e-7f * (2.0f * X + rsum + P.lmax) / (rs * c23);
+  const float xi = x / c23;
+  if (xi < kJkrXiNeg - m) return false;
+  if (xi > m && xi < kJkrXiPos - m) return false;
+  const float f1 = logf(rs);
+  if (f1 < P.jdom_lo[1] || f1 > P.jdom_hi[1]) return false;
+  if (sqrtf(fmaxf(xi - m + kJkrKappa, 0.0f)) > P.jdom_hi[0]) return false;
+  return true;
+}
+
+// Whether a JKR pair is certainly in the ZERO region of jkr_certify (no
+// contact radius makes the reference's residual smaller than 1e-3 R*, so its
+// JKR force is exactly zero), decided on the FP32 position mirror with that
+// mirror's rounding added to the certificate's margin. Symmetric in (i, j)
+// bit for bit, so both ends of a pair drop it or keep it together.
+__device__ __forceinline__ bool jkr_far_zero(const StepParams& P, float4 xif, float Xi, float4 xjf) {
+  float fx = xif.x - xjf.x, fy = xif.y - xjf.y, fz = xif.z - xjf.z;
+  if (P.periodic[0]) { const float L = (float)P.bsize[0]; if (fx > 0.5f * L) fx -= L; else if (fx < -0.5f * L) fx += L; }
+  if (P.periodic[1]) { const float L = (float)P.bsize[1]; if (fy > 0.5f * L) fy -= L; else if (fy < -0.5f * L) fy += L; }
+  if (P.periodic[2]) { const float L = (float)P.bsize[2]; if (fz > 0.5f * L) fz -= L; else if (fz < -0.5f * L) fz += L; }
+  const float rsum = xif.w + xjf.w;
+  const float rs = (xif.w * xjf.w) / rsum;
+  const float c = P.jkr_Cf / rs;
+  if (!(c > 0.0f && c < 1e30f)) return false;
+  const float c23 = jkr_c23(c);
+  const float d = sqrtf(fx * fx + fy * fy + fz * fz);
+  const float X = fmaxf(Xi, fmaxf(fmaxf(fabsf(xjf.x), fabsf(xjf.y)), fabsf(xjf.z)));
+  // per-axis FP32 difference error <= 6e-8 (2X + 2 cut + L) (as in pretest_far),
+  // so |d_f - d| <= 1.8e-7 (2X + 3 r_sum + L) + 4e-7 d, radii rounded too
+  const float e = (1.8e-7f * (2.0f * X + 3.0f * rsum + P.lmax) + 4e-7f * (d + rsum)) / rs;
+  const float x = (rsum - d) / rs;
+  return x + kJkrKappa * c23 + 1e-3f < -(1e-5f * (fabsf(x) + c23 + 1e-3f) + 2.0f * e);
+}
+
 // Pass 1 (FP32 and integer work only): the candidates of each particle, i.e.
 // list entries the FP32 pretest cannot rule out and that the reference's loop
 // visits from this end (visit counts from both ends recorded); counts all
@@ -651,9 +826,17 @@ __global__ void __launch_bounds__(128) k_contact_filter(StepParams P) {
   if (C->halt) return;
   const Bank B = P.bank[C->bank];
   const bool adh = (P.nmodel == 3 || P.nmodel == 4);
+  const bool learn = P.jkr_solver == 1 && P.nmodel == 3 && P.gamma_pp > 0.0 && P.mlp != nullptr;
+  // Certified-zero JKR pairs add exactly +-0 to F and T when the tangential
+  // force then vanishes too (Coulomb with |F_n| = 0; physical-mode springs
+  // reset out of contact): with the certified solvers they are not
+  // candidates at all. Parity-mode springs (G* = 0, NaN for Mindlin at
+  // negative overlap) and debug recording keep every pair.
+  const bool zdrop = P.jkr_solver != 0 && P.nmodel == 3 && P.gamma_pp > 0.0 && P.pretest && !P.debug &&
+                     (P.tmodel == 0 || PHYS);
   const size_t plane = (size_t)P.n * P.cap;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < P.n; k += gridDim.x * blockDim.x) {
-    uint32_t nrec = 0, ncmp = 0;
+    uint32_t nrec = 0, ncmp = 0, nnet = 0;
     if (!(B.flags[k] & PF_DEAD)) {
       const unsigned long long ci = PHYS ? 0ull : (unsigned long long)__double_as_longlong(B.wc[k].w);
       const float4 xif = B.xf[k];
@@ -665,7 +848,8 @@ __global__ void __launch_bounds__(128) k_contact_filter(StepParams P) {
         const uint32_t j = row[m];
         const size_t hi = (size_t)k * P.cap + m;
         int vij = 0, vji = 0;
-        if (!(P.pretest && pretest_far(P, xif, Xi, B.xf[j], adh))) {
+        const float4 xjf = B.xf[j];
+        if (!(P.pretest && pretest_far(P, xif, Xi, xjf, adh)) && !(zdrop && jkr_far_zero(P, xif, Xi, xjf))) {
           if (PHYS) {
             vij = vji = 1;
           } else {
@@ -675,9 +859,12 @@ __global__ void __launch_bounds__(128) k_contact_filter(StepParams P) {
           }
         }
         if (vij > 0) {
-          out[nrec] = CRec{j, m | ((uint32_t)vij << 16) | ((uint32_t)vji << 24)};
+          const bool evaluates = !(vji > 0 && (uint32_t)k > j);
+          const uint32_t net = (learn && evaluates && jkr_net_hint(P, xif, xjf)) ? CREC_NET : 0u;
+          out[nrec] = CRec{j, m | ((uint32_t)vij << 16) | ((uint32_t)vji << 24) | net};
           ++nrec;
-          if (!(vji > 0 && (uint32_t)k > j)) ++ncmp;
+          if (evaluates) ++ncmp;
+          if (net) ++nnet;
         } else {
           if (HIST) {
             B.hist[hi] = 0.0;
@@ -690,20 +877,86 @@ __global__ void __launch_bounds__(128) k_contact_filter(StepParams P) {
     }
     P.ccnt[k] = nrec;
     P.ncomp[k] = ncmp;
+    if (learn) P.nnet[k] = nnet;
   }
 }
 
-// Pass 2: the compact list of evaluating records.
+// Pass 2: the compact list of evaluating records, and the network queue (in
+// particle order, at the offsets of the scan of the per-particle counts).
 __global__ void __launch_bounds__(256) k_contact_index(StepParams P) {
   if (P.ctrl->halt) return;
+  const bool learn = P.jkr_solver == 1 && P.nmodel == 3 && P.gamma_pp > 0.0 && P.mlp != nullptr;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < P.n; k += gridDim.x * blockDim.x) {
     const uint32_t n = P.ccnt[k];
     uint32_t q = P.poff[k];
+    uint32_t qn = learn ? P.noff[k] : 0u;
     const size_t base = (size_t)k * P.cap;
     for (uint32_t c = 0; c < n; ++c) {
       const CRec r = P.crec[base + c];
-      if (!((r.mv >> 24) > 0 && (uint32_t)k > r.j)) P.clist[q++] = (uint32_t)(base + c);
+      if (!(crec_vji(r.mv) > 0 && (uint32_t)k > r.j)) {
+        if (r.mv & CREC_NET) P.jq[qn++] = make_uint2(q, (uint32_t)(base + c));
+        P.clist[q++] = (uint32_t)(base + c);
+      }
     }
+  }
+}
+
+// Pass 2b: the JKR network over the queue, 32 pairs per warp on the tensor
+// cores (weights staged once per block in shared memory). Features from the
+// FP64 positions: the overlap from r_sum^2 - d^2 in FP64, the rest in FP32.
+// Writes the predicted a/R* of each queued pair, NaN outside the training
+// range.
+__global__ void __launch_bounds__(128) k_jkr_mlp(StepParams P) {
+  Ctrl* C = P.ctrl;
+  if (C->halt) return;
+  const uint32_t qn = P.ctot[2];
+  if ((uint32_t)blockIdx.x * blockDim.x >= qn) return;
+  __shared__ MlpInfer M;
+  {
+    const uint4* src = reinterpret_cast<const uint4*>(P.mlp);
+    uint4* dst = reinterpret_cast<uint4*>(&M);
+    for (int i = threadIdx.x; i < (int)(sizeof(MlpInfer) / 16); i += blockDim.x) dst[i] = src[i];
+  }
+  __syncthreads();
+  const Bank B = P.bank[C->bank];
+  const int lane = threadIdx.x & 31;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  const float es = (float)P.es_pp, gam = (float)P.gamma_pp;
+  const float les = logf(es), lgam = logf(gam);
+  for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < qn; base += stride) {
+    const uint32_t idx = base + lane;
+    const bool valid = idx < qn;
+    float f[4] = {0.f, 0.f, 0.f, 0.f};
+    float ub = 0.f;
+    bool ok = false;
+    uint32_t q = 0;
+    if (valid) {
+      const uint2 it = P.jq[idx];
+      q = it.x;
+      const uint32_t s = it.y;
+      const uint32_t k = s / (uint32_t)P.cap;
+      const uint32_t j = P.crec[s].j;
+      const D4 xi4 = B.xr[k], xj4 = B.xr[j];
+      const V d = mic(P, xyz(xi4) - xyz(xj4));
+      const double d2 = dot(d, d);
+      const double rsum = xi4.w + xj4.w;
+      const float ov = (float)(rsum * rsum - d2) / ((float)rsum + sqrtf((float)d2));
+      const float rs = (float)(xi4.w * xj4.w / rsum);
+      const float x = ov / rs;
+      const float c = P.jkr_Cf / rs;
+      const float c23 = jkr_c23(c);
+      // the features of jkr_raw_features, with ln E* and ln gamma hoisted
+      const float raw[4] = {jkr_overlap_feature(x, c23), logf(rs), les, lgam};
+      ok = true;
+#pragma unroll
+      for (int a = 0; a < 4; ++a) {
+        ok = ok && raw[a] >= P.jdom_lo[a] && raw[a] <= P.jdom_hi[a];
+        f[a] = (raw[a] - M.xmean[a]) * M.xinv[a];
+      }
+      ub = jkr_ubase(x, c23);
+    }
+    const float y = mlp_forward_warp(&M, f);
+    if (valid) P.jguess[q] = ok ? __expf(y * M.ystd + M.ymean) * ub : __int_as_float(0x7FC00000);
   }
 }
 
@@ -723,12 +976,15 @@ __global__ void __launch_bounds__(128) k_contact_force(StepParams P) {
   const uint32_t total = P.ctot[1];
   const bool adh = (P.nmodel == 3 || P.nmodel == 4);
   bool excess = false;
+  uint32_t tally[6] = {0u, 0u, 0u, 0u, 0u, 0u};
   for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
     const uint32_t s = P.clist[t];
     const uint32_t k = s / (uint32_t)P.cap, c = s - k * (uint32_t)P.cap;
     const CRec r = P.crec[s];
     const uint32_t j = r.j, m = r.mv & 0xFFFFu;
-    const int vij = (r.mv >> 16) & 0xFF, vji = r.mv >> 24;
+    const int vij = (r.mv >> 16) & 0xFF, vji = crec_vji(r.mv);
+    const float guess = (r.mv & CREC_NET) ? P.jguess[t] : -1.0f;
+    if (r.mv & CREC_NET) tally[3] += 1;
     const D4 xi4 = B.xr[k], xj4 = B.xr[j];
     const V d = mic(P, xyz(xi4) - xyz(xj4));
     const double d2 = dot(d, d);
@@ -741,9 +997,9 @@ __global__ void __launch_bounds__(128) k_contact_force(StepParams P) {
     if (in) {
       const D4 vi4 = B.vm[k], wi4 = B.wc[k], vj4 = B.vm[j], wj4 = B.wc[j];
       if (!pair_contact<R, PHYS, HIST>(P, d, d2, rsum, xi4.w, xj4.w, vi4.w, vj4.w, xyz(vi4), xyz(vj4), xyz(wi4),
-                                       xyz(wj4), hk, plane, fc, tc, nrm, excess))
+                                       xyz(wj4), hk, plane, fc, tc, nrm, excess, guess, tally))
         pair_contact<double, PHYS, HIST>(P, d, d2, rsum, xi4.w, xj4.w, vi4.w, vj4.w, xyz(vi4), xyz(vj4), xyz(wi4),
-                                         xyz(wj4), hk, plane, fc, tc, nrm, excess);
+                                         xyz(wj4), hk, plane, fc, tc, nrm, excess, guess);
     } else if (HIST) {
       hk[0] = 0.0;
       hk[plane] = 0.0;
@@ -783,6 +1039,14 @@ __global__ void __launch_bounds__(128) k_contact_force(StepParams P) {
     }
   }
   if (excess) C->overlap_flag = 1;
+  if (P.jkr_solver != 0 && P.nmodel == 3) {
+    __syncwarp();
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+      const uint32_t v = __reduce_add_sync(0xFFFFFFFFu, tally[q]);
+      if ((threadIdx.x & 31) == 0 && v) atomicAdd(&C->jkr_count[q], (unsigned long long)v);
+    }
+  }
 }
 
 // Pass 4: per particle, the contact results in list order, the walls, then
@@ -896,13 +1160,23 @@ static int launch_contact_path(const StepParams& P, cudaStream_t s) {
   else k_contact_filter<true, false><<<g, 128, 0, s>>>(P);
   launch_exclusive_scan(nullptr, P.ccnt, P.coff, (uint32_t)P.n, P.cpart, P.ctot, s);
   launch_exclusive_scan(nullptr, P.ncomp, P.poff, (uint32_t)P.n, P.cpart, P.ctot + 1, s);
+  const bool learn = P.jkr_solver == 1 && P.nmodel == 3 && P.gamma_pp > 0.0 && P.mlp != nullptr;
+  int launched = 10;
+  if (learn) {
+    launch_exclusive_scan(nullptr, P.nnet, P.noff, (uint32_t)P.n, P.cpart, P.ctot + 2, s);
+    launched += 3;
+  }
   k_contact_index<<<grid_for(P.n, 256), 256, 0, s>>>(P);
+  if (learn) {
+    k_jkr_mlp<<<152 * 4, 128, 0, s>>>(P);
+    ++launched;
+  }
   const int gc = grid_for((uint64_t)P.n * 4, 128);
   if (P.mode == 0) k_contact_force<false, false, R><<<gc, 128, 0, s>>>(P);
   else if (hist) k_contact_force<true, true, R><<<gc, 128, 0, s>>>(P);
   else k_contact_force<true, false, R><<<gc, 128, 0, s>>>(P);
   k_accumulate<<<g, 128, 0, s>>>(P);
-  return 10;
+  return launched;
 }
 
 int launch_force(const StepParams& P, cudaStream_t s) {

@@ -542,4 +542,160 @@ int rp_debug_reference_grid(rp_sim* s, double h, int64_t* cell_of, int64_t* orde
   return s->e->debug_reference_grid(h, cell_of, order, n_order, dims);
 }
 
+// ---------------------------------------------------------- learned JKR
+int rp_jkr_train(rp_sim* s, const rp_jkr_train_options* options, rp_jkr_train_report* report) {
+  SIM_OR_FAIL(s);
+  return s->e->jkr_train(options, report);
+}
+int rp_set_jkr_solver(rp_sim* s, int solver) {
+  SIM_OR_FAIL(s);
+  if (solver != RP_JKR_NEWTON && solver != RP_JKR_LEARNED && solver != RP_JKR_CERTIFIED) {
+    set_error("unknown JKR solver %d", solver);
+    return RP_E_INVALID_ARG;
+  }
+  if (solver == RP_JKR_LEARNED && !s->e->jkr_has_network()) {
+    set_error("the learned JKR solver needs a network (rp_jkr_train or rp_jkr_set_network)");
+    return RP_E_INVALID_ARG;
+  }
+  s->e->jkr_solver = solver;
+  s->e->config_changed();
+  return RP_OK;
+}
+int rp_jkr_get_network(rp_sim* s, float* params, float* norm, float* domain) {
+  SIM_OR_FAIL(s);
+  return s->e->jkr_get_network(params, norm, domain);
+}
+int rp_jkr_set_network(rp_sim* s, const float* params, const float* norm, const float* domain) {
+  SIM_OR_FAIL(s);
+  if (!params || !norm || !domain) {
+    set_error("null network buffer");
+    return RP_E_INVALID_ARG;
+  }
+  return s->e->jkr_set_network(params, norm, domain);
+}
+int rp_jkr_counters(rp_sim* s, uint64_t out[6]) {
+  SIM_OR_FAIL(s);
+  if (!out) {
+    set_error("null output");
+    return RP_E_INVALID_ARG;
+  }
+  return s->e->jkr_counters(out);
+}
+
+}  // extern "C"
+
+namespace {
+
+int need_device() {
+  int cnt = 0;
+  cudaError_t e = cudaGetDeviceCount(&cnt);
+  if (e != cudaSuccess || cnt == 0) {
+    rp::set_error("no usable CUDA device: %s", e != cudaSuccess ? cudaGetErrorString(e) : "device count is 0");
+    return RP_E_CUDA;
+  }
+  return RP_OK;
+}
+
+// Device copies of host arrays for the standalone network entry points.
+struct DevBufs {
+  std::vector<void*> ptrs;
+  ~DevBufs() {
+    for (void* p : ptrs) cudaFree(p);
+  }
+  template <typename T>
+  T* get(size_t n, const T* src) {
+    void* p = nullptr;
+    if (cudaMalloc(&p, sizeof(T) * std::max<size_t>(n, 1)) != cudaSuccess) return nullptr;
+    ptrs.push_back(p);
+    if (src && n && cudaMemcpy(p, src, sizeof(T) * n, cudaMemcpyHostToDevice) != cudaSuccess) return nullptr;
+    return (T*)p;
+  }
+};
+
+int cuda_fail(const char* what) {
+  rp::set_error("%s failed: %s", what, cudaGetErrorString(cudaGetLastError()));
+  return RP_E_CUDA;
+}
+
+}  // namespace
+
+extern "C" {
+
+int rp_mlp_loss_grad(const float* params, const float* features, const float* targets, const float* weights, size_t n,
+                     int qat, float* grad, double* loss) {
+  if (!params || !features || !targets || !weights || !grad || !loss || n < 64 || (n & (n - 1)) != 0) {
+    set_error("rp_mlp_loss_grad needs all buffers and n a power of two >= 64");
+    return RP_E_INVALID_ARG;
+  }
+  int r = need_device();
+  if (r) return r;
+  DevBufs B;
+  float* p = B.get(rp::MLP_NPARAM, params);
+  float* f = B.get(4 * n, features);
+  float* t = B.get(n, targets);
+  float* w = B.get(n, weights);
+  float* g = B.get<float>(rp::MLP_NPARAM, nullptr);
+  if (!p || !f || !t || !w || !g) return cuda_fail("device allocation");
+  if (rp::mlp_loss_grad(p, f, t, w, n, qat, g, loss, 0) != 0) return cuda_fail("network gradient");
+  if (cudaMemcpy(grad, g, sizeof(float) * rp::MLP_NPARAM, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return cuda_fail("gradient copy");
+  return RP_OK;
+}
+
+int rp_mlp_infer(const float* params, const float* features, size_t n, float* out) {
+  if (!params || !features || !out) {
+    set_error("null buffer");
+    return RP_E_INVALID_ARG;
+  }
+  int r = need_device();
+  if (r) return r;
+  rp::MlpInfer h;
+  const float norm[10] = {0, 0, 0, 0, 1, 1, 1, 1, 0, 1};
+  rp::mlp_make_infer(params, norm, &h);
+  DevBufs B;
+  rp::MlpInfer* m = B.get(1, &h);
+  float* f = B.get(4 * n, features);
+  float* o = B.get<float>(n, nullptr);
+  if (!m || !f || !o) return cuda_fail("device allocation");
+  if (rp::mlp_infer_rows(m, f, n, o, 0) != 0) return cuda_fail("network inference");
+  if (n && cudaMemcpy(out, o, sizeof(float) * n, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return cuda_fail("output copy");
+  return RP_OK;
+}
+
+int rp_jkr_samples(const double domain[8], uint64_t seed, size_t n, float* features, float* targets, float* weights,
+                   double* a_ref, int32_t* iters, double* inputs) {
+  if (!domain || !features || !targets || !weights) {
+    set_error("null buffer");
+    return RP_E_INVALID_ARG;
+  }
+  for (int k = 0; k < 6; ++k)
+    if (!(domain[k] > 0.0)) {
+      set_error("domain radius, modulus and surface-energy bounds must be positive");
+      return RP_E_INVALID_ARG;
+    }
+  int r = need_device();
+  if (r) return r;
+  rp::JkrDomain D{domain[0], domain[1], domain[2], domain[3], domain[4], domain[5], domain[6], domain[7]};
+  DevBufs B;
+  float* f = B.get<float>(4 * n, nullptr);
+  float* t = B.get<float>(n, nullptr);
+  float* w = B.get<float>(n, nullptr);
+  double* a = a_ref ? B.get<double>(n, nullptr) : nullptr;
+  int32_t* it = iters ? B.get<int32_t>(n, nullptr) : nullptr;
+  double* in = inputs ? B.get<double>(4 * n, nullptr) : nullptr;
+  if (!f || !t || !w || (a_ref && !a) || (iters && !it) || (inputs && !in)) return cuda_fail("device allocation");
+  if (rp::jkr_generate_samples(D, seed, n, f, t, w, a, it, in, 0) != 0) return cuda_fail("sample generation");
+  if (n) {
+    if (cudaMemcpy(features, f, sizeof(float) * 4 * n, cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(targets, t, sizeof(float) * n, cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(weights, w, sizeof(float) * n, cudaMemcpyDeviceToHost) != cudaSuccess ||
+        (a_ref && cudaMemcpy(a_ref, a, sizeof(double) * n, cudaMemcpyDeviceToHost) != cudaSuccess) ||
+        (iters && cudaMemcpy(iters, it, sizeof(int32_t) * n, cudaMemcpyDeviceToHost) != cudaSuccess) ||
+        (inputs && cudaMemcpy(inputs, in, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost) != cudaSuccess))
+      return cuda_fail("sample copy");
+  }
+  return RP_OK;
+}
+
 }  // extern "C"

@@ -39,6 +39,10 @@ struct Ctrl {
   int pad_;
   unsigned long long target;      // device step loop: run while steps_done < target
   unsigned long long iters;       // device step loop iterations (bounded by target + 4)
+  // learned JKR tallies (pair evaluations): network/certified-solver results
+  // accepted, certified zeros, reference-Newton fallbacks, network rows, FP32
+  // Newton steps, closed-form walks
+  unsigned long long jkr_count[6];
 };
 
 struct Material {
@@ -70,14 +74,20 @@ struct TriRec {
   double a, b, c, det, denom, pad;
   float4 plane;  // unit normal from the vertices and n.v0, FP32 (zero for a degenerate triangle)
   float4 bound;  // .x = largest |vertex coordinate| (scales the FP32 plane-test error)
+  float4 edge[3];  // per edge: in-plane outward unit normal m and m.(edge start); (0,0,0,1e30) if degenerate
 };
 
 // A contact candidate kept by the filter: neighbour slot, row position and
-// the reference's visit counts from both ends (m | vis_ij << 16 | vis_ji << 24).
+// the reference's visit counts from both ends (m | vis_ij << 16 | vis_ji << 24,
+// visit counts <= 27), bit 31 set when the pair is queued for the JKR network.
+constexpr uint32_t CREC_NET = 0x80000000u;
+__host__ __device__ __forceinline__ int crec_vji(uint32_t mv) { return (int)((mv >> 24) & 0x7Fu); }
 struct CRec {
   uint32_t j;
   uint32_t mv;
 };
+
+struct MlpInfer;
 
 struct StepParams {
   int n;  // slots
@@ -90,7 +100,7 @@ struct StepParams {
   uint32_t* coff;   // exclusive scan of ccnt: result offset of particle k
   uint32_t* poff;   // exclusive scan of ncomp
   uint32_t* clist;  // compact list of evaluating record slots
-  uint32_t* ctot;   // [0] records, [1] evaluating records
+  uint32_t* ctot;   // [0] records, [1] evaluating records, [2] network queue
   double* cres;     // per record: force (3) and torque (3) on the row's particle
   uint32_t* cpart;  // scan partials
   int nmodel, tmodel, mode, prec;
@@ -104,7 +114,7 @@ struct StepParams {
   double gamma_pp, gamma_pw;   // combined surface energies
   double beta_abs;             // |ln e / sqrt(ln^2 e + pi^2)| of the particle restitution (host libm)
   // reference grid (parity-mode visit rule)
-  double href;
+  double href, inv_href;
   int rdims[3];
   // fine grid (neighbour search)
   double fmin[3], fcell[3];
@@ -122,6 +132,17 @@ struct StepParams {
   int tdims[3];
   const uint32_t* tstart;
   const uint32_t* titems;
+  // JKR solver for particle pairs: 0 the reference's Newton, 1 certificates +
+  // network + polish, 2 certificates + FP32 Newton from the reference's start
+  int jkr_solver;
+  double jkr_C;  // 8 pi gamma / E* of particle pairs, as the reference forms it
+  float jkr_Cf;
+  float jdom_lo[4], jdom_hi[4];  // raw-feature range of the training set
+  const MlpInfer* mlp;
+  uint2* jq;        // network queue: (evaluating index, record slot); length ctot[2]
+  uint32_t* nnet;   // queued records per particle
+  uint32_t* noff;   // exclusive scan of nnet
+  float* jguess;    // per evaluating index: predicted a/R* (NaN = outside the training range)
   // diagnostics
   double* dbgF;
   double* dbgT;
@@ -159,11 +180,23 @@ __device__ __forceinline__ int32_t code_axis(unsigned long long c, int k) {
   return (v << 11) >> 11;  // sign-extend 21 bits
 }
 
+// floor(d / h) with the correctly rounded quotient, from the product with the
+// rounded reciprocal: d * rd(1/h) lies within 3 u |d/h| (u = 2^-53) of rd(d/h),
+// so the two floors agree unless the product is within 8 u |q| of an integer;
+// only then is the division itself evaluated.
+__device__ __forceinline__ double floor_div_exact(double d, double h, double inv_h) {
+  const double q = dmul(d, inv_h);
+  const double f = floor(q);
+  const double tol = 8.8817841970012523e-16 * fabs(q);  // 8 u |q|
+  if (q - f <= tol || dsub(f + 1.0, q) <= tol) return floor(d / h);
+  return f;
+}
+
 // Reference cell coordinates of a position (src/grid.rs:30-32).
 __device__ __forceinline__ void ref_coords(const StepParams& P, double x, double y, double z, int32_t c[3]) {
-  c[0] = sat_i32(floor(dsub(x, P.bmin[0]) / P.href));
-  c[1] = sat_i32(floor(dsub(y, P.bmin[1]) / P.href));
-  c[2] = sat_i32(floor(dsub(z, P.bmin[2]) / P.href));
+  c[0] = sat_i32(floor_div_exact(dsub(x, P.bmin[0]), P.href, P.inv_href));
+  c[1] = sat_i32(floor_div_exact(dsub(y, P.bmin[1]), P.href, P.inv_href));
+  c[2] = sat_i32(floor_div_exact(dsub(z, P.bmin[2]), P.href, P.inv_href));
 }
 
 // Number of times the reference's 27-cell loop (src/grid.rs:54-85) lists the
