@@ -195,7 +195,137 @@ def adhesive_workload(n=4_194_304, seed=2027, phi=0.35):
     }
 
 
+def batched_workload(n_boxes=512, seed=2028, phi=0.45, n_lo=2000, n_hi=60000):
+    """n_boxes independent walled boxes, each with a particle count drawn
+    log-uniform in [n_lo, n_hi], radii U[0.5, 1.5] mm, sJKR + Coulomb,
+    surface energy U[0, 0.1] J/m^2 per box (E = 1e7 Pa, nu = 0.3, rho = 2500,
+    mu = 0.5, e = 0.5), box side giving solid fraction phi, dt = 1e-6 s; the
+    boxes sit on an 8 x 8 x 8 grid of slots with gaps wider than any cutoff.
+    Each box is one group (its own bed, material and 12 wall triangles)."""
+    rng = np.random.default_rng(seed)
+    counts = np.exp(rng.uniform(np.log(n_lo), np.log(n_hi), n_boxes)).astype(np.int64)
+    gammas = rng.uniform(0.0, 0.1, n_boxes)
+    radii = [rng.uniform(0.5e-3, 1.5e-3, c) for c in counts]
+    sides = np.array([(float((4.0 / 3.0 * np.pi * r ** 3).sum()) / phi) ** (1.0 / 3.0) for r in radii])
+    slot = float(sides.max()) + 0.006
+    per = math.ceil(n_boxes ** (1.0 / 3.0))
+    from tests.stl_util import box_tris
+    xs, rs, gs, tv, tn, tg = [], [], [], [], [], []
+    for b in range(n_boxes):
+        i, j, k = b % per, (b // per) % per, b // (per * per)
+        lo = np.array([i, j, k], float) * slot + 0.003
+        side = sides[b]
+        m = math.ceil(counts[b] ** (1.0 / 3.0))
+        sp = side / m
+        g = np.stack(np.meshgrid(*[np.arange(m)] * 3, indexing="ij"), -1).reshape(-1, 3)
+        g = g[rng.permutation(len(g))[:counts[b]]]
+        g = g[np.lexsort((g[:, 2], g[:, 0], g[:, 1]))]
+        xs.append(lo + (g + 0.5) * sp)
+        rs.append(radii[b])
+        gs.append(np.full(counts[b], b, np.uint32))
+        for t in box_tris(lo, lo + side):
+            nv = np.cross(t[1] - t[0], t[2] - t[0])
+            tv.append(np.concatenate(t))
+            tn.append(nv / np.linalg.norm(nv))
+            tg.append(b)
+    r = np.concatenate(rs)
+    top = per * slot + 0.006
+    return {
+        "name": f"batched-{n_boxes}", "lo": (0.0, 0.0, 0.0), "hi": (top, top, top), "periodic": (False, False, False),
+        "dt": 1e-6, "normal": "sjkr", "tangential": "coulomb", "material": (1e7, 0.3, 2500.0, 0.5, 0.5, gammas[0]),
+        "tri_v": np.asarray(tv, np.float32), "tri_n": np.asarray(tn, np.float32), "tri_group": np.asarray(tg),
+        "position": np.concatenate(xs), "radius": r, "mass": 2500.0 * 4.0 / 3.0 * np.pi * r ** 3,
+        "groups": np.concatenate(gs), "counts": counts,
+        "group_material": [(1e7, 0.3, 2500.0, 0.5, 0.5, float(gm)) for gm in gammas],
+        "describe": (f"{n_boxes} independent walled boxes, {int(counts.sum()):,} spheres in all (per box log-uniform "
+                     f"in [{n_lo:,}, {n_hi:,}]), radii U[0.5,1.5] mm, sJKR+Coulomb, surface energy U[0,0.1] J/m^2 "
+                     f"per box, solid fraction {phi}, dt=1e-6 s, all boxes stepped by one device loop"),
+    }
+
+
+def drum_triangles(R, L, n_theta=256, n_z=117, n_rings=5):
+    """Closed cylinder about the z axis (radius R, z in [0, L]): n_theta x n_z
+    wall quads, and per end cap a 256-triangle fan plus n_rings rings of
+    n_theta quads; normals point inward. 256*117*2 + 2*256*11 = 65,536."""
+    th = np.linspace(0.0, 2.0 * np.pi, n_theta + 1)
+    zs = np.linspace(0.0, L, n_z + 1)
+    c, s = np.cos(th), np.sin(th)
+    tris = []
+    for j in range(n_z):
+        for i in range(n_theta):
+            p00 = (R * c[i], R * s[i], zs[j]); p01 = (R * c[i + 1], R * s[i + 1], zs[j])
+            p10 = (R * c[i], R * s[i], zs[j + 1]); p11 = (R * c[i + 1], R * s[i + 1], zs[j + 1])
+            tris += [(p00, p01, p10), (p01, p11, p10)]
+    rr = np.linspace(0.0, R, n_rings + 2)
+    for z in (0.0, L):
+        for i in range(n_theta):
+            tris.append(((0.0, 0.0, z), (rr[1] * c[i], rr[1] * s[i], z), (rr[1] * c[i + 1], rr[1] * s[i + 1], z)))
+        for k in range(1, n_rings + 1):
+            for i in range(n_theta):
+                a0 = (rr[k] * c[i], rr[k] * s[i], z); a1 = (rr[k] * c[i + 1], rr[k] * s[i + 1], z)
+                b0 = (rr[k + 1] * c[i], rr[k + 1] * s[i], z); b1 = (rr[k + 1] * c[i + 1], rr[k + 1] * s[i + 1], z)
+                tris += [(a0, b0, a1), (a1, b0, b1)]
+    v = np.asarray(tris, np.float64).reshape(-1, 9)
+    a, b, cc = v[:, 0:3], v[:, 3:6], v[:, 6:9]
+    n = np.cross(b - a, cc - a)
+    n /= np.linalg.norm(n, axis=1, keepdims=True)
+    centre = (a + b + cc) / 3.0
+    inward = np.stack([-centre[:, 0], -centre[:, 1], L / 2 - centre[:, 2]], 1)
+    flip = (n * inward).sum(1) < 0
+    v[flip] = np.concatenate([a[flip], cc[flip], b[flip]], 1)
+    n[flip] = -n[flip]
+    return v.astype(np.float32), n.astype(np.float32)
+
+
+def drum_workload(n=16_777_216, seed=2029, R=0.5, rpm=30.0, fill=0.4):
+    """Rotating drum: n spheres, radii U[1, 2] mm, Hertz + Coulomb, E = 1e7 Pa,
+    nu = 0.3, rho = 2500, restitution 0.3, friction 0.4, in a closed drum of
+    radius R about the z axis turning at `rpm` (the 65,536-triangle wall moves
+    with omega x p), filled to `fill` of its volume, dt = 5e-6 s. The drum
+    length follows from the fill: n spheres of this size fill 40 % of a
+    0.5 m x 1.7 m drum (a 0.3 m drum holds about 3.5 M of them). Start: a
+    shuffled cubic lattice in the lower segment at 0.6x radii grown by `relax`."""
+    rng = np.random.default_rng(seed)
+    r = rng.uniform(1e-3, 2e-3, n)
+    sp = (float((4.0 / 3.0 * np.pi * r ** 3).mean()) / 0.5) ** (1.0 / 3.0)  # lattice at solid fraction 0.5
+    area = fill * np.pi * R * R
+    lo_y, hi_y = -R, R
+    for _ in range(80):  # fill height of the circular segment with that area
+        y = 0.5 * (lo_y + hi_y)
+        seg = R * R * math.acos(-y / R) + y * math.sqrt(max(R * R - y * y, 0.0))
+        lo_y, hi_y = (y, hi_y) if seg < area else (lo_y, y)
+    yf = 0.5 * (lo_y + hi_y)
+    rin = R - 2.5e-3
+    kx = np.arange(-math.ceil(R / sp), math.ceil(R / sp) + 1)
+    gx, gy = np.meshgrid(kx * sp, kx * sp, indexing="ij")
+    ok = (gx ** 2 + gy ** 2 < rin ** 2) & (gy < yf)
+    xy = np.stack([gx[ok], gy[ok]], 1)
+    layers = math.ceil(n / len(xy))
+    L = layers * sp + 6e-3
+    z = 3e-3 + (np.arange(layers) + 0.5) * sp
+    sites = np.concatenate([np.column_stack([xy, np.full(len(xy), zz)]) for zz in z])
+    sites = sites[rng.permutation(len(sites))[:n]]
+    sites = sites[np.lexsort((sites[:, 0], sites[:, 1], sites[:, 2]))]
+    x = sites + rng.uniform(-0.02, 0.02, sites.shape) * sp
+    v, nn = drum_triangles(R, L)
+    w = 2.0 * np.pi * rpm / 60.0
+    m = 0.02
+    return {
+        "name": "drum-16M" if n == 16_777_216 else f"drum-{n}",
+        "lo": (-R - m, -R - m, -m), "hi": (R + m, R + m, L + m), "periodic": (False, False, False),
+        "dt": 5e-6, "normal": "hertz", "tangential": "coulomb", "material": (1e7, 0.3, 2500.0, 0.4, 0.3, 0.0),
+        "tri_v": v, "tri_n": nn, "tri_motion": ((0.0, 0.0, 0.0), (0.0, 0.0, w), (0.0, 0.0, 0.0)),
+        "position": x, "radius": r, "mass": 2500.0 * 4.0 / 3.0 * np.pi * r ** 3,
+        "describe": (f"{n:,} spheres, radii U[1,2] mm, Hertz+Coulomb, E=1e7 Pa, e=0.3, mu=0.4, rotating drum "
+                     f"R={R} m x L={L:.2f} m ({len(v):,} triangles, {rpm:g} rpm about z), fill {fill}, dt=5e-6 s"),
+    }
+
+
 def make_workload(args):
+    if args.workload == "drum":
+        return drum_workload(n=args.particles or 16_777_216)
+    if args.workload == "batched":
+        return batched_workload(n_boxes=args.boxes)
     if args.workload == "hopper":
         return hopper_workload(n=args.particles or 1_048_576)
     if args.workload == "adhesive":
@@ -211,12 +341,52 @@ def make_sim(rp, wl, mode="parity", precision="fp64"):
     s.set_particle_material(*wl["material"])
     s.set_contact_models(wl["normal"], wl["tangential"])
     s.set_periodic_boundary(*wl["periodic"])
-    if len(wl["tri_v"]):
-        s.add_triangles(wl["tri_v"], wl["tri_n"])
+    if "tri_group" in wl:
+        for g in range(len(wl["group_material"])):
+            sel = wl["tri_group"] == g
+            s.add_triangles(wl["tri_v"][sel], wl["tri_n"][sel], group=g)
+    elif len(wl["tri_v"]):
+        s.add_triangles(wl["tri_v"], wl["tri_n"], motion=wl.get("tri_motion"))
     s.add_particles(wl["position"], wl["radius"], wl["mass"])
+    if "groups" in wl:
+        s.set_particle_groups(wl["groups"])
+        for g, m in enumerate(wl["group_material"]):
+            s.set_group_material(g, *m)
     if "velocity" in wl:
         s.set_state({"velocity": wl["velocity"]})
     return s
+
+
+def one_box_workload(wl, b):
+    """Box b of a batched workload as its own single-group workload."""
+    sel = wl["groups"] == b
+    tsel = wl["tri_group"] == b
+    return {
+        "name": f"box-{b}", "lo": wl["lo"], "hi": wl["hi"], "periodic": wl["periodic"], "dt": wl["dt"],
+        "normal": wl["normal"], "tangential": wl["tangential"], "material": wl["group_material"][b],
+        "tri_v": wl["tri_v"][tsel], "tri_n": wl["tri_n"][tsel], "position": wl["position"][sel],
+        "radius": wl["radius"][sel], "mass": wl["mass"][sel],
+    }
+
+
+def one_at_a_time(rp, wl, steps, n_sample=16, log=None):
+    """Particle-steps/s when the boxes are stepped as separate simulations (one
+    device loop per box, same engine), on a sample of boxes spread over the
+    size range, extrapolated by total particle-steps over total device time."""
+    order = np.argsort(wl["counts"], kind="stable")
+    pick = order[np.linspace(0, len(order) - 1, min(n_sample, len(order))).astype(int)]
+    units, ms = 0, 0.0
+    for b in pick:
+        s = make_sim(rp, one_box_workload(wl, int(b)))
+        s.steps(3)
+        a = s.stats()
+        s.steps(steps)
+        c = s.stats()
+        units += int(c["particles"]) * steps
+        ms += c["device_ms"] - a["device_ms"]
+        del s
+    return {"value": units / (ms / 1e3), "boxes_timed": int(len(pick)), "steps_each": steps,
+            "sample": "boxes at evenly spaced size quantiles, each its own Simulation (device loop)"}
 
 
 def relax(rp, wl, stages=9, steps_per_stage=100, settle=300, log=None):
@@ -470,7 +640,7 @@ def run_ours(args, log):
     n = len(wl["radius"])
     if args.state_in:
         wl["position"] = np.load(args.state_in)["position"]
-    elif args.workload in ("hopper", "adhesive"):
+    elif args.workload in ("hopper", "adhesive", "batched", "drum"):
         relax(rp, wl, log=log)
     if args.state_out:
         np.savez(args.state_out, position=wl["position"])
@@ -483,9 +653,20 @@ def run_ours(args, log):
         solver = args.jkr_solver or "learned"
         jkr = {"solver": solver}
         if solver == "learned":
-            jkr["training"] = sim.train_jkr_network(seed=1)
+            if args.jkr_net_in:
+                z = np.load(args.jkr_net_in)
+                sim.set_jkr_network(z["params"], z["norm"], z["domain"])
+                jkr["network"] = f"loaded from {os.path.basename(args.jkr_net_in)}"
+            else:
+                jkr["training"] = sim.train_jkr_network(seed=1)
+            if args.jkr_net_out:
+                p, nm, dm = sim.get_jkr_network()
+                np.savez(args.jkr_net_out, params=p, norm=nm, domain=dm)
         sim.set_jkr_solver(solver)
     sim.steps(args.warmup)
+    tune = None
+    if args.autotune or (args.workload == "batched" and not args.no_autotune):
+        tune = sim.autotune()
     torch.cuda.synchronize()
     s0 = sim.stats()
     c0 = sim.jkr_counters() if jkr else None
@@ -571,6 +752,11 @@ def run_ours(args, log):
     }
     if jkr:
         line["config"]["jkr"] = jkr
+    if tune:
+        line["config"]["autotune"] = tune
+    if args.workload == "batched":
+        line["config"]["boxes"] = int(len(wl["counts"]))
+        line["config"]["one_at_a_time"] = one_at_a_time(rp, wl, min(args.steps, 100))
     print(json.dumps(line), flush=True)
     barrier(dist)
     return 0
@@ -582,9 +768,14 @@ def main():
     ap.add_argument("--steps", type=int, default=500)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["hopper", "box", "adhesive"], default="hopper")
+    ap.add_argument("--workload", choices=["hopper", "box", "adhesive", "batched", "drum"], default="hopper")
+    ap.add_argument("--boxes", type=int, default=512, help="boxes of the batched workload")
+    ap.add_argument("--autotune", action="store_true", help="autotune launch shapes before timing")
+    ap.add_argument("--no-autotune", action="store_true", help="batched workload: keep default launch shapes")
     ap.add_argument("--jkr-solver", choices=["newton", "learned", "certified"], default=None,
                     help="JKR solver of the adhesive workload (default learned)")
+    ap.add_argument("--jkr-net-in", default=None, help="trained JKR network (.npz) instead of training")
+    ap.add_argument("--jkr-net-out", default=None, help="save the trained JKR network (.npz)")
     ap.add_argument("--mode", choices=["parity", "physical"], default="parity")
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
     ap.add_argument("--no-cpu", action="store_true")

@@ -197,6 +197,48 @@ int rp_debug_contact_pairs(rp_sim* sim, int64_t* pi, int64_t* pj, int32_t* visit
 int rp_debug_reference_grid(rp_sim* sim, double h, int64_t* cell_of, int64_t* order, size_t* n_order,
                             int32_t dims[3]);
 
+/* --- groups: independent beds stepped together (no counterpart in the
+ * reference, which simulates one bed per Simulation). A group is what one
+ * reference Simulation would hold: its particles interact only with each other
+ * and with the group's triangles (or those added for all groups), under the
+ * group's particle material; dt, models, gravity, bounds and the wall
+ * material are shared. Group 0 uses rp_set_particle_material. With every
+ * particle in group 0 (the default) nothing changes. */
+#define RP_GROUP_ALL 0xFFFFFFFFu
+/* groups[i] for particle id i (n = rp_particle_count), each < 2^24. */
+int rp_set_particle_groups(rp_sim* sim, size_t n, const uint32_t* groups);
+int rp_get_particle_groups(rp_sim* sim, size_t n, uint32_t* groups);
+/* The particle material of one group (as rp_set_particle_material). */
+int rp_set_group_material(rp_sim* sim, uint32_t group, double youngs_modulus, double poissons_ratio, double density,
+                          double friction_coefficient, double restitution_coefficient, double surface_energy);
+/* rp_add_mesh_triangles for the particles of one group (RP_GROUP_ALL: every group). */
+int rp_add_mesh_triangles_group(rp_sim* sim, size_t n_triangles, const float* vertices, const float* normals,
+                                uint32_t group);
+
+/* --- moving walls (no counterpart in the reference, whose walls are static):
+ * triangles whose surface moves with velocity + omega x (p - center) while the
+ * geometry stays (a drum turning about its own axis, a belt). The wall enters
+ * each contact's relative velocity at the contact point. */
+int rp_add_mesh_triangles_moving(rp_sim* sim, size_t n_triangles, const float* vertices, const float* normals,
+                                 uint32_t group, const double center[3], const double omega[3],
+                                 const double velocity[3]);
+
+/* --- launch shapes of the force pass (no counterpart in the reference) */
+typedef struct rp_tune_report {
+  int32_t force_path; /* 0 contact-parallel, 1 one thread per particle */
+  int32_t bs_filter, bs_force, bs_accum; /* threads per block */
+  int32_t grid_cap;   /* largest grid of the grid-stride loops */
+  int32_t candidates; /* configurations timed */
+  double default_ms, best_ms; /* median force-pass time, default and chosen shape */
+} rp_tune_report;
+/* Times the force pass on the current state for candidate shapes (block
+ * sizes 64/128/256 per kernel, grid caps, the per-particle path) and keeps
+ * the fastest. The state is not changed. Needs one completed step; not
+ * available in physical mode with a spring history. report may be NULL. */
+int rp_autotune(rp_sim* sim, rp_tune_report* report);
+/* Sets the shapes directly (0 = default: 128 threads, 152*64 blocks). */
+int rp_set_launch_shape(rp_sim* sim, int bs_filter, int bs_force, int bs_accum, int grid_cap);
+
 /* --- learned JKR contact radius (no counterpart in the reference; replaces
  * the per-contact Newton iteration of src/physics.rs:164-191 for particle
  * pairs of the JKR model)

@@ -252,6 +252,11 @@ V3<T> linear_spring_coulomb(T fn, V3<T> rv, V3<T> n, V3<T>& xi, T kt, T mu, T dt
 template <typename T>
 struct Triangle {  // src/mesh.rs:5-16
   V3<T> v0, v1, v2, n;
+  int motion = -1;  // extension: index of a rigid surface velocity (-1: static, the reference's walls)
+};
+// Extension: the surface velocity V + W x (p - C) of a moving wall.
+struct WallMotion {
+  double c[3], w[3], v[3];
 };
 // src/mesh.rs:45-117 (region tests as in the reference, including its
 // swapped (-e).clamp(0, c) assignment to s in the t<0 / a+d<=b+e branch)
@@ -296,8 +301,9 @@ V3<T> closest_point(const Triangle<T>& tr, V3<T> p) {
 }
 // src/mesh.rs:20-43
 template <typename T>
-bool intersect_sphere(const Triangle<T>& tr, V3<T> c, T r, T& pen, V3<T>& n) {
+bool intersect_sphere(const Triangle<T>& tr, V3<T> c, T r, T& pen, V3<T>& n, V3<T>* cp_out = nullptr) {
   V3<T> cp = closest_point(tr, c);
+  if (cp_out) *cp_out = cp;
   V3<T> dv = c - cp;
   T d2 = dv.length_squared();
   if (d2 < r * r) {
@@ -321,6 +327,7 @@ struct Sim : Base {
   bool periodic[3] = {false, false, false};
   std::vector<Particle<T>> ps;
   std::vector<Triangle<T>> tris;
+  std::vector<WallMotion> motions;
   Material<T> pm{T(1e7), T(0.3), T(2500), T(0.5), T(0.5), T(0)};   // src/simulation.rs:69
   Material<T> wm{T(1e9), T(0.3), T(7800), T(0.5), T(0.5), T(0)};   // src/simulation.rs:70
   int nmodel = N_HERTZ, tmodel = T_MINDLIN;                         // src/simulation.rs:84-85
@@ -683,12 +690,18 @@ struct Sim : Base {
       }
       // particle-mesh (src/simulation.rs:464-523)
       for (const Triangle<T>& tr : tris) {
-        T pen; V3<T> nrm;
-        if (!intersect_sphere(tr, p.x, p.r, pen, nrm)) continue;
+        T pen; V3<T> nrm, cp;
+        if (!intersect_sphere(tr, p.x, p.r, pen, nrm, &cp)) continue;
         if (pen > T(0.2) * p.r) excessive = true;
         V3<T> ra = -nrm * p.r;
         V3<T> va = p.v + p.w.cross(ra);
         V3<T> rv = va;
+        if (tr.motion >= 0) {  // extension: the wall surface moves with V + W x (cp - C)
+          const WallMotion& M = motions[tr.motion];
+          const V3<T> arm = cp - V3<T>((T)M.c[0], (T)M.c[1], (T)M.c[2]);
+          const V3<T> vw = V3<T>((T)M.v[0], (T)M.v[1], (T)M.v[2]) + V3<T>((T)M.w[0], (T)M.w[1], (T)M.w[2]).cross(arm);
+          rv = rv - vw;
+        }
         T rs = p.r, ms = p.m;
         tl_terms = 0.0;
         V3<T> fnv;
@@ -820,6 +833,31 @@ void orc_add_triangles(void* hv, const double* v, const double* nrm, long nt) {
       t.v1 = V3<T>((T)q[3], (T)q[4], (T)q[5]);
       t.v2 = V3<T>((T)q[6], (T)q[7], (T)q[8]);
       t.n = V3<T>((T)nrm[3 * k], (T)nrm[3 * k + 1], (T)nrm[3 * k + 2]);
+      s->tris.push_back(t);
+    }
+    return 0;
+  });
+}
+// Extension: triangles whose surface moves with V + W x (p - C).
+void orc_add_triangles_moving(void* hv, const double* v, const double* nrm, long nt, const double* c9) {
+  dispatch((Handle*)hv, [&](auto* s) {
+    using T = decltype(s->dt);
+    WallMotion m;
+    for (int k = 0; k < 3; ++k) {
+      m.c[k] = c9[k];
+      m.w[k] = c9[3 + k];
+      m.v[k] = c9[6 + k];
+    }
+    s->motions.push_back(m);
+    const int id = (int)s->motions.size() - 1;
+    for (long k = 0; k < nt; ++k) {
+      Triangle<T> t;
+      const double* q = v + 9 * k;
+      t.v0 = V3<T>((T)q[0], (T)q[1], (T)q[2]);
+      t.v1 = V3<T>((T)q[3], (T)q[4], (T)q[5]);
+      t.v2 = V3<T>((T)q[6], (T)q[7], (T)q[8]);
+      t.n = V3<T>((T)nrm[3 * k], (T)nrm[3 * k + 1], (T)nrm[3 * k + 2]);
+      t.motion = id;
       s->tris.push_back(t);
     }
     return 0;

@@ -59,6 +59,7 @@ def lib():
             "orc_get_threads": (i, []),
             "orc_add_particle": (None, [vp, d, d, d, d, d, i]),
             "orc_add_triangles": (None, [vp, dp, dp, l]),
+            "orc_add_triangles_moving": (None, [vp, dp, dp, l, dp]),
             "orc_set_material": (None, [vp, i, d, d, d, d, d, d]),
             "orc_set_models": (None, [vp, i, i]),
             "orc_set_periodic": (None, [vp, i, i, i]),
@@ -177,10 +178,16 @@ class OracleSimulation:
         v, n = read_stl(path)
         self.add_triangles(v, n)
 
-    def add_triangles(self, v, n):
+    def add_triangles(self, v, n, motion=None):
+        """motion = (center, omega, velocity): the surface moves with
+        velocity + omega x (p - center) (an extension; None = static walls)."""
         v = np.ascontiguousarray(v, np.float64).reshape(-1, 9)
         n = np.ascontiguousarray(n, np.float64).reshape(-1, 3)
-        self._L.orc_add_triangles(self._h, _dp(v), _dp(n), len(v))
+        if motion is None:
+            self._L.orc_add_triangles(self._h, _dp(v), _dp(n), len(v))
+        else:
+            c9 = np.ascontiguousarray(np.concatenate([np.asarray(m, np.float64).ravel() for m in motion]))
+            self._L.orc_add_triangles_moving(self._h, _dp(v), _dp(n), len(v), _dp(c9))
 
     def step(self):
         self._L.orc_step(self._h, 1)

@@ -89,13 +89,49 @@ class Simulation:
         """src/lib.rs:87-91: binary or ASCII STL; IOError on failure."""
         check(self._L.rp_add_mesh_stl(self._h, str(path).encode()))
 
-    def add_triangles(self, vertices, normals=None):
-        """Triangles as a [T,9] array (no reference counterpart)."""
+    def add_triangles(self, vertices, normals=None, group=None, motion=None):
+        """Triangles as a [T,9] array (no reference counterpart); `group`
+        restricts them to the particles of one group; `motion` = (center,
+        omega, velocity) gives their surface the velocity
+        velocity + omega x (p - center) (the geometry stays put)."""
         v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 9)
         n = None if normals is None else np.ascontiguousarray(normals, np.float32).reshape(-1, 3)
         fp = ctypes.POINTER(ctypes.c_float)
-        check(self._L.rp_add_mesh_triangles(self._h, len(v), v.ctypes.data_as(fp),
-                                            n.ctypes.data_as(fp) if n is not None else None))
+        nptr = n.ctypes.data_as(fp) if n is not None else None
+        if motion is not None:
+            c, w, u = (np.ascontiguousarray(a, np.float64).reshape(3) for a in motion)
+            g = _lib.RP_GROUP_ALL if group is None else int(group)
+            check(self._L.rp_add_mesh_triangles_moving(self._h, len(v), v.ctypes.data_as(fp), nptr, g, _dptr(c),
+                                                       _dptr(w), _dptr(u)))
+        elif group is None:
+            check(self._L.rp_add_mesh_triangles(self._h, len(v), v.ctypes.data_as(fp), nptr))
+        else:
+            check(self._L.rp_add_mesh_triangles_group(self._h, len(v), v.ctypes.data_as(fp), nptr, int(group)))
+
+    # ---- launch shapes ------------------------------------------------------
+    def autotune(self):
+        """Choose the force pass's launch shapes on the current state (after a step)."""
+        r = _lib.RpTuneReport()
+        check(self._L.rp_autotune(self._h, ctypes.byref(r)))
+        return {k: getattr(r, k) for k, _ in _lib.RpTuneReport._fields_}
+
+    def set_launch_shape(self, bs_filter=0, bs_force=0, bs_accum=0, grid_cap=0):
+        check(self._L.rp_set_launch_shape(self._h, int(bs_filter), int(bs_force), int(bs_accum), int(grid_cap)))
+
+    # ---- groups: independent beds in one simulation -----------------------
+    def set_particle_groups(self, groups):
+        g = np.ascontiguousarray(groups, np.uint32)
+        check(self._L.rp_set_particle_groups(self._h, g.size, g.ctypes.data_as(_lib._u32p)))
+
+    def get_particle_groups(self):
+        g = np.zeros(self.get_particle_count(), np.uint32)
+        check(self._L.rp_get_particle_groups(self._h, g.size, g.ctypes.data_as(_lib._u32p)))
+        return g
+
+    def set_group_material(self, group, youngs_modulus, poissons_ratio, density, friction_coefficient,
+                           restitution_coefficient, surface_energy):
+        check(self._L.rp_set_group_material(self._h, int(group), youngs_modulus, poissons_ratio, density,
+                                            friction_coefficient, restitution_coefficient, surface_energy))
 
     def step(self):
         """src/lib.rs:94."""

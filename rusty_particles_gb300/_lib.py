@@ -68,6 +68,21 @@ RP_JKR_NEWTON, RP_JKR_LEARNED, RP_JKR_CERTIFIED = 0, 1, 2
 RP_MLP_PARAMS = 8705
 _fp = ctypes.POINTER(ctypes.c_float)
 _u64p = ctypes.POINTER(ctypes.c_uint64)
+_u32p = ctypes.POINTER(ctypes.c_uint32)
+RP_GROUP_ALL = 0xFFFFFFFF
+
+
+class RpTuneReport(ctypes.Structure):
+    _fields_ = [
+        ("force_path", ctypes.c_int32),
+        ("bs_filter", ctypes.c_int32),
+        ("bs_force", ctypes.c_int32),
+        ("bs_accum", ctypes.c_int32),
+        ("grid_cap", ctypes.c_int32),
+        ("candidates", ctypes.c_int32),
+        ("default_ms", ctypes.c_double),
+        ("best_ms", ctypes.c_double),
+    ]
 
 
 class RpJkrTrainOptions(ctypes.Structure):
@@ -149,6 +164,14 @@ SIGNATURES = {
                                                ctypes.POINTER(ctypes.c_size_t), _i32p]),
     "rp_cell_sort_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_size_t, _dp, ctypes.c_double, _i32p,
                                             ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "rp_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(RpTuneReport)]),
+    "rp_set_launch_shape": (ctypes.c_int, [ctypes.c_void_p] + [ctypes.c_int] * 4),
+    "rp_add_mesh_triangles_group": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_size_t, _fp, _fp, ctypes.c_uint32]),
+    "rp_add_mesh_triangles_moving": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_size_t, _fp, _fp, ctypes.c_uint32,
+                                                    _dp, _dp, _dp]),
+    "rp_set_particle_groups": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_size_t, _u32p]),
+    "rp_get_particle_groups": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_size_t, _u32p]),
+    "rp_set_group_material": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32] + [ctypes.c_double] * 6),
     "rp_jkr_train": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(RpJkrTrainOptions),
                                     ctypes.POINTER(RpJkrTrainReport)]),
     "rp_set_jkr_solver": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),

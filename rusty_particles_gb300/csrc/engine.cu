@@ -48,6 +48,25 @@ static double physical_shear(double e1, double nu1, double e2, double nu2) {
   double g1 = shear_mod(e1, nu1), g2 = shear_mod(e2, nu2);
   return 1.0 / ((2.0 - nu1) / g1 + (2.0 - nu2) / g2);
 }
+// Law constants of one particle material against the wall material
+// (src/material.rs:33-50, src/physics.rs:112-116, 165).
+Law Engine::make_law(const Material& m) const {
+  Law L;
+  std::memset(&L, 0, sizeof(L));
+  L.es_pp = eff_youngs(m.E, m.nu, m.E, m.nu);
+  L.es_pw = eff_youngs(m.E, m.nu, wm.E, wm.nu);
+  L.gs_pp = mode == RP_MODE_PARITY ? 0.0 : physical_shear(m.E, m.nu, m.E, m.nu);
+  L.gamma_pp = (m.gamma + m.gamma) * 0.5;
+  L.gamma_pw = (m.gamma + wm.gamma) * 0.5;
+  const double ln_e = std::log(m.e);
+  const double beta = ln_e / std::sqrt(ln_e * ln_e + kPiH * kPiH);
+  L.beta_abs = std::fabs(beta);
+  L.mu = m.mu;
+  L.jkr_C = (8.0 * kPiH) * L.gamma_pp / L.es_pp;
+  L.jkr_Cf = (float)L.jkr_C;
+  return L;
+}
+
 static int bits_for(uint64_t maxkey) {
   int b = 1;
   while (b < 32 && (1ull << b) <= maxkey) ++b;
@@ -95,6 +114,7 @@ void Engine::free_device() {
     Bank& B = bank_[b];
     dfree(B.xr); dfree(B.vm); dfree(B.wc); dfree(B.acc); dfree(B.tq);
     dfree(B.xres); dfree(B.vres); dfree(B.wres); dfree(B.flags); dfree(B.tag); dfree(B.xref); dfree(B.xf);
+    dfree(B.grp);
     dfree(B.nbr); dfree(B.ncnt); dfree(B.hist);
   }
   dfree(rb_.ka); dfree(rb_.va); dfree(rb_.kb); dfree(rb_.vb); dfree(rb_.hist); dfree(rb_.part);
@@ -102,9 +122,10 @@ void Engine::free_device() {
   dfree(dbgF_); dfree(dbgT_); dfree(dbgMult_); dfree(ke_);
   dfree(crec_); dfree(clist_); dfree(cres_); dfree(ccnt_); dfree(ncomp_); dfree(coff_); dfree(poff_);
   dfree(ctot_); dfree(cpart_);
-  dfree(tri_d_); dfree(tstart_d_); dfree(titems_d_);
-  dfree(mlp_d_); dfree(jq_); dfree(jguess_); dfree(nnet_); dfree(noff_);
+  dfree(tri_d_); dfree(tstart_d_); dfree(titems_d_); dfree(glaw_d_); dfree(motions_d_);
+  dfree(mlp_d_); dfree(jq_); dfree(jguess_); dfree(nnet_); dfree(noff_); dfree(jfb_);
   jq_alloc_ = 0;
+  jfb_alloc_ = 0;
   dfree(ctrl_);
   if (ctrl_h_) cudaFreeHost(ctrl_h_);
   ctrl_h_ = nullptr;
@@ -183,9 +204,16 @@ int Engine::add_particle(const double x[3], double r, double m, int fixed) {
   return RP_OK;
 }
 
-int Engine::add_triangles(size_t n, const float* v, const float* nrm) {
+int Engine::add_triangles(size_t n, const float* v, const float* nrm, uint32_t group, const WallMotion* motion) {
+  uint32_t mid = NO_MOTION;
+  if (motion && n > 0) {
+    motions_.push_back(*motion);
+    mid = (uint32_t)(motions_.size() - 1);
+  }
   for (size_t t = 0; t < n; ++t) {
     const float* q = v + 9 * t;
+    tri_group_.push_back(group);
+    tri_motion_.push_back(mid);
     for (int k = 0; k < 9; ++k) tri_v_.push_back(q[k]);
     if (nrm) {
       for (int k = 0; k < 3; ++k) tri_n_.push_back(nrm[3 * t + k]);
@@ -196,6 +224,52 @@ int Engine::add_triangles(size_t n, const float* v, const float* nrm) {
       double l = std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
       for (int k = 0; k < 3; ++k) tri_n_.push_back(l > 0 ? (float)(c[k] / l) : 0.f);
     }
+  }
+  dev_valid_ = false;
+  return RP_OK;
+}
+
+int Engine::set_particle_groups(size_t n, const uint32_t* groups) {
+  if (!host_valid_) TRY(download());
+  if (n != hp_.size()) {
+    set_error("group array has %zu entries for %zu particles", n, hp_.size());
+    return RP_E_INVALID_ARG;
+  }
+  for (size_t i = 0; i < n; ++i) {
+    if (groups[i] >= (1u << 24)) {
+      set_error("group id %u too large (at most 2^24 - 1)", groups[i]);
+      return RP_E_INVALID_ARG;
+    }
+  }
+  for (size_t i = 0; i < n; ++i) hp_[i].group = groups[i];
+  dev_valid_ = false;
+  return RP_OK;
+}
+
+int Engine::get_particle_groups(size_t n, uint32_t* groups) {
+  if (!host_valid_) TRY(download());
+  if (n != hp_.size()) {
+    set_error("group array has %zu entries for %zu particles", n, hp_.size());
+    return RP_E_INVALID_ARG;
+  }
+  for (size_t i = 0; i < n; ++i) groups[i] = hp_[i].group;
+  return RP_OK;
+}
+
+int Engine::set_group_material(uint32_t group, const Material& m) {
+  if (group >= (1u << 24)) {
+    set_error("group id %u too large (at most 2^24 - 1)", group);
+    return RP_E_INVALID_ARG;
+  }
+  if (group == 0) {
+    pm = m;
+  } else {
+    if (gmat_.size() <= group) {
+      gmat_.resize(group + 1, pm);
+      gmat_set_.resize(group + 1, 0);
+    }
+    gmat_[group] = m;
+    gmat_set_[group] = 1;
   }
   dev_valid_ = false;
   return RP_OK;
@@ -217,7 +291,7 @@ int Engine::alloc_slots(size_t n) {
     TRY(dalloc(&B.xr, na)); TRY(dalloc(&B.vm, na)); TRY(dalloc(&B.wc, na)); TRY(dalloc(&B.acc, na));
     TRY(dalloc(&B.tq, na)); TRY(dalloc(&B.xres, na)); TRY(dalloc(&B.vres, na)); TRY(dalloc(&B.wres, na));
     TRY(dalloc(&B.flags, na)); TRY(dalloc(&B.tag, na)); TRY(dalloc(&B.xref, na)); TRY(dalloc(&B.ncnt, na));
-    TRY(dalloc(&B.xf, na));
+    TRY(dalloc(&B.xf, na)); TRY(dalloc(&B.grp, na));
   }
   TRY(dalloc(&rb_.ka, na)); TRY(dalloc(&rb_.va, na)); TRY(dalloc(&rb_.kb, na)); TRY(dalloc(&rb_.vb, na));
   TRY(dalloc(&kraw_, na));
@@ -227,7 +301,8 @@ int Engine::alloc_slots(size_t n) {
   TRY(dalloc(&dbgF_, 3 * na)); TRY(dalloc(&dbgT_, 3 * na));
   TRY(dalloc(&ccnt_, na)); TRY(dalloc(&ncomp_, na)); TRY(dalloc(&coff_, na)); TRY(dalloc(&poff_, na));
   TRY(dalloc(&nnet_, na)); TRY(dalloc(&noff_, na));
-  TRY(dalloc(&ctot_, 3)); TRY(dalloc(&cpart_, scan_parts_needed((uint32_t)na) + 16));
+  TRY(dalloc(&ctot_, 4)); TRY(dalloc(&cpart_, scan_parts_needed((uint32_t)na) + 16));
+  CK(cudaMemset(ctot_, 0, 4 * sizeof(uint32_t)));
   n_alloc_ = na;
   // lists must be re-allocated for the new slot count
   for (int b = 0; b < 2; ++b) {
@@ -289,6 +364,19 @@ int Engine::alloc_lists(int cap, bool keep_current) {
 // evaluating record) and the device copy of the network, for the learned
 // JKR solver only.
 int Engine::ensure_jkr_buffers() {
+  // pairs left to the reference's Newton by the certified solvers, in FP64
+  const bool defer = gpu_ && jkr_solver != RP_JKR_NEWTON && nmodel == RP_NORMAL_JKR && prec == RP_PREC_FP64;
+  if (defer) {
+    const size_t need = std::max<size_t>(n_alloc_ * (size_t)std::max(cap_, 1), 1);
+    if (jfb_alloc_ < need) {
+      TRY(dalloc(&jfb_, need));
+      jfb_alloc_ = need;
+      graph_dirty_ = true;
+    }
+    P_.jfb = jfb_;
+  } else {
+    P_.jfb = nullptr;
+  }
   if (jkr_solver != RP_JKR_LEARNED || !gpu_ || !jkr_have_net_) {
     P_.mlp = nullptr;
     return RP_OK;
@@ -350,15 +438,22 @@ int Engine::build_params() {
   }
   P.pm = pm;
   P.wm = wm;
-  P.es_pp = eff_youngs(pm.E, pm.nu, pm.E, pm.nu);
-  P.es_pw = eff_youngs(pm.E, pm.nu, wm.E, wm.nu);
-  P.gs_pp = mode == RP_MODE_PARITY ? 0.0 : physical_shear(pm.E, pm.nu, pm.E, pm.nu);
-  P.gamma_pp = (pm.gamma + pm.gamma) * 0.5;
-  P.gamma_pw = (pm.gamma + wm.gamma) * 0.5;
+  // per-group law constants (group 0: the particle material)
   {
-    double ln_e = std::log(pm.e);
-    double beta = ln_e / std::sqrt(ln_e * ln_e + kPiH * kPiH);
-    P.beta_abs = std::fabs(beta);
+    uint32_t ng = 1;
+    for (const HostParticle& p : hp_) ng = std::max(ng, p.group + 1);
+    for (uint32_t g : tri_group_)
+      if (g != GROUP_ALL) ng = std::max(ng, g + 1);
+    std::vector<Law> laws(ng);
+    for (uint32_t g = 0; g < ng; ++g) {
+      const Material& m = (g > 0 && g < gmat_.size() && gmat_set_[g]) ? gmat_[g] : pm;
+      laws[g] = make_law(m);
+    }
+    P.law = laws[0];
+    P.ngroups = (int)ng;
+    TRY(dalloc(&glaw_d_, ng));
+    CK(cudaMemcpy(glaw_d_, laws.data(), sizeof(Law) * ng, cudaMemcpyHostToDevice));
+    P.glaw = glaw_d_;
   }
   // reference grid: dims = ceil(size / h) + 1 (src/grid.rs:13)
   P.href = href;
@@ -426,10 +521,11 @@ int Engine::build_params() {
   P.dbgT = dbgT_;
   P.ctrl = ctrl_;
   P.force_path = force_path;
-  // JKR of particle pairs: C = 8 pi gamma / E* as src/physics.rs:165 forms it
+  P.bs_filter = bs_filter;
+  P.bs_force = bs_force;
+  P.bs_accum = bs_accum;
+  P.grid_cap = grid_cap;
   P.jkr_solver = jkr_solver;
-  P.jkr_C = (8.0 * kPiH) * P.gamma_pp / P.es_pp;
-  P.jkr_Cf = (float)P.jkr_C;
   for (int k = 0; k < 4; ++k) {
     P.jdom_lo[k] = jkr_dom_[k];
     P.jdom_hi[k] = jkr_dom_[4 + k];
@@ -447,11 +543,17 @@ int Engine::build_params() {
 int Engine::build_triangle_grid(double rmax) {
   const size_t T = tri_v_.size() / 9;
   P_.ntri = (int)T;
+  P_.motions = nullptr;
   if (T == 0) {
     P_.tri = nullptr;
     P_.tstart = nullptr;
     P_.titems = nullptr;
     return RP_OK;
+  }
+  if (!motions_.empty()) {
+    TRY(dalloc(&motions_d_, motions_.size()));
+    CK(cudaMemcpy(motions_d_, motions_.data(), sizeof(WallMotion) * motions_.size(), cudaMemcpyHostToDevice));
+    P_.motions = motions_d_;
   }
   std::vector<TriRec> recs(T);
   double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
@@ -477,7 +579,8 @@ int Engine::build_triangle_grid(double rmax) {
     r.c = r.e1[0] * r.e1[0] + r.e1[1] * r.e1[1] + r.e1[2] * r.e1[2];
     r.det = r.a * r.c - r.b * r.b;
     r.denom = r.a - 2.0 * r.b + r.c;
-    r.pad = 0.0;
+    r.group = t < tri_group_.size() ? tri_group_[t] : GROUP_ALL;
+    r.motion = t < tri_motion_.size() ? tri_motion_[t] : NO_MOTION;
     {
       double cx = r.e0[1] * r.e1[2] - r.e0[2] * r.e1[1], cy = r.e0[2] * r.e1[0] - r.e0[0] * r.e1[2],
              cz = r.e0[0] * r.e1[1] - r.e0[1] * r.e1[0];
@@ -605,9 +708,10 @@ int Engine::upload() {
   const size_t na = std::max<size_t>(n, 1);
   std::vector<D4> a8[8];
   for (auto& v : a8) v.resize(na);
-  std::vector<uint32_t> flags(na, 0), tags(na, 0);
+  std::vector<uint32_t> flags(na, 0), tags(na, 0), groups(na, 0);
   for (size_t i = 0; i < n; ++i) {
     const HostParticle& p = hp_[i];
+    groups[i] = p.group;
     a8[0][i] = D4{p.x[0], p.x[1], p.x[2], p.r};
     a8[1][i] = D4{p.v[0], p.v[1], p.v[2], p.m};
     a8[2][i] = D4{p.w[0], p.w[1], p.w[2], 0.0};
@@ -627,6 +731,7 @@ int Engine::upload() {
     for (int q = 0; q < 8; ++q) CK(cudaMemcpy(dst[q], a8[q].data(), sizeof(D4) * n, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(B.flags, flags.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(B.tag, tags.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(B.grp, groups.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice));
     std::vector<float4> xref(n, make_float4(NAN, NAN, NAN, 0.f));
     CK(cudaMemcpy(B.xref, xref.data(), sizeof(float4) * n, cudaMemcpyHostToDevice));
     for (size_t i = 0; i < n; ++i)
@@ -665,7 +770,7 @@ int Engine::download() {
   const size_t n = (size_t)n_;
   std::vector<D4> a8[8];
   const D4* src[8] = {B.xr, B.vm, B.wc, B.acc, B.tq, B.xres, B.vres, B.wres};
-  std::vector<uint32_t> flags(n), tags(n);
+  std::vector<uint32_t> flags(n), tags(n), groups(n, 0u);
   if (n > 0) {
     for (int q = 0; q < 8; ++q) {
       a8[q].resize(n);
@@ -673,6 +778,7 @@ int Engine::download() {
     }
     CK(cudaMemcpy(flags.data(), B.flags, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(tags.data(), B.tag, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost));
+    if (P_.ngroups > 1) CK(cudaMemcpy(groups.data(), B.grp, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost));
   }
   std::vector<std::pair<uint32_t, size_t>> order;
   order.reserve(n);
@@ -701,6 +807,7 @@ int Engine::download() {
     p.m = a8[1][k].w;
     p.fixed = (flags[k] & PF_FIXED) ? 1 : 0;
     p.tag = tags[k];
+    p.group = groups[k];
   }
   host_valid_ = true;
   if (dead) dev_valid_ = false;  // the next step re-uploads the compacted set
@@ -808,18 +915,21 @@ int Engine::build_graph() {
 }
 
 int Engine::launch_steps_graph(uint64_t n) {
-  if (graph_dirty_ || !graph_exec_) {
-    int r = build_graph();
-    if (r != RP_OK) {
-      // conditional graph nodes unavailable: fall back to host-issued steps
-      destroy_graph();
-      use_graph_ = false;
-      cudaGetLastError();
-      return launch_steps(n);
-    }
-  }
   uint64_t remaining = n;
   while (remaining > 0) {
+    // The graph bakes in the kernel parameters (buffer pointers, list
+    // capacity): recover_halt reallocates the lists, so it is rebuilt before
+    // every launch that follows a change.
+    if (graph_dirty_ || !graph_exec_) {
+      int r = build_graph();
+      if (r != RP_OK) {
+        // conditional graph nodes unavailable: host-issued steps instead
+        destroy_graph();
+        use_graph_ = false;
+        cudaGetLastError();
+        return launch_steps(remaining);
+      }
+    }
     const uint64_t before = last_.steps_done, rb_before = last_.rebuilds;
     unsigned long long lim[2] = {before + remaining, 0ull};  // target, iters
     CK(cudaMemcpyAsync(&ctrl_->target, &lim[0], sizeof(unsigned long long), cudaMemcpyHostToDevice, stream_));
@@ -1142,6 +1252,113 @@ int Engine::debug_reference_grid(double h, int64_t* cell_of, int64_t* order, siz
     if (sk[k] < ncells) order[m++] = (int64_t)sv[k];
   *n_order = m;
   // the device upload used the sort buffers: the next step rebuilds anyway
+  return RP_OK;
+}
+
+// ------------------------------------------------------------- autotuner
+// Chooses the force pass's launch shapes on the current state: the pass only
+// reads the state and rewrites a, tau and its scratch buffers, so it can be
+// timed repeatedly (CUDA events on the engine's stream, median of 5 after 2
+// warm-up passes). Coordinate descent over the filter, pair and accumulate
+// block sizes (64, 128, 256), the grid cap of their grid-stride loops, then the
+// one-thread-per-particle path. The control block (counters, flags) is
+// restored afterwards. Needs lists (a step already taken); the physical mode's
+// spring history is rewritten by the pass, so that mode is not tuned.
+int Engine::autotune(rp_tune_report* rep) {
+  if (rep) std::memset(rep, 0, sizeof(*rep));
+  TRY(ensure_gpu());
+  if (!dev_valid_) {
+    set_error("step at least once before autotuning (the force pass needs neighbour lists)");
+    return RP_E_INVALID_ARG;
+  }
+  TRY(sync_ctrl());
+  if (ctrl_h_->steps_done == 0 || ctrl_h_->rebuild || ctrl_h_->halt || n_ == 0) {
+    set_error("step at least once before autotuning (the force pass needs neighbour lists)");
+    return RP_E_INVALID_ARG;
+  }
+  if (mode == RP_MODE_PHYSICAL && tmodel != RP_TANGENTIAL_COULOMB) {
+    set_error("the physical mode's spring history would change: not tuned");
+    return RP_E_INVALID_ARG;
+  }
+  Ctrl saved;
+  std::memcpy(&saved, ctrl_h_, sizeof(Ctrl));
+  int tried = 0;
+  auto time_pass = [&](float* out) -> int {
+    for (int w = 0; w < 2; ++w) launch_force(P_, stream_);
+    float t[5];
+    for (int r = 0; r < 5; ++r) {
+      CK(cudaEventRecord(ev0_, stream_));
+      launch_force(P_, stream_);
+      CK(cudaEventRecord(ev1_, stream_));
+      CK(cudaEventSynchronize(ev1_));
+      CK(cudaEventElapsedTime(&t[r], ev0_, ev1_));
+    }
+    CK(cudaGetLastError());
+    std::sort(t, t + 5);
+    *out = t[2];
+    ++tried;
+    return RP_OK;
+  };
+  int cfg[5] = {0, 128, 128, 128, 152 * 64};  // path, filter, pair, accumulate, grid cap
+  auto apply = [&](const int c[5]) {
+    P_.force_path = c[0];
+    P_.bs_filter = c[1];
+    P_.bs_force = c[2];
+    P_.bs_accum = c[3];
+    P_.grid_cap = c[4];
+  };
+  apply(cfg);
+  float best = 0.f;
+  TRY(time_pass(&best));
+  const float def_ms = best;
+  const int blocks[3] = {64, 128, 256};
+  const int caps[3] = {152 * 4, 152 * 16, 152 * 64};
+  for (int dim = 1; dim <= 4; ++dim) {
+    for (int k = 0; k < 3; ++k) {
+      int c[5];
+      std::memcpy(c, cfg, sizeof(c));
+      c[dim] = dim == 4 ? caps[k] : blocks[k];
+      if (c[dim] == cfg[dim]) continue;
+      apply(c);
+      float t = 0.f;
+      TRY(time_pass(&t));
+      if (t < best) {
+        best = t;
+        std::memcpy(cfg, c, sizeof(c));
+      }
+    }
+  }
+  {
+    int c[5];
+    std::memcpy(c, cfg, sizeof(c));
+    c[0] = 1;
+    apply(c);
+    float t = 0.f;
+    TRY(time_pass(&t));
+    if (t < best) {
+      best = t;
+      cfg[0] = 1;
+    }
+  }
+  apply(cfg);
+  force_path = cfg[0];
+  bs_filter = cfg[1];
+  bs_force = cfg[2];
+  bs_accum = cfg[3];
+  grid_cap = cfg[4];
+  CK(cudaMemcpy(ctrl_, &saved, sizeof(Ctrl), cudaMemcpyHostToDevice));
+  TRY(sync_ctrl());
+  graph_dirty_ = true;
+  if (rep) {
+    rep->force_path = cfg[0];
+    rep->bs_filter = cfg[1];
+    rep->bs_force = cfg[2];
+    rep->bs_accum = cfg[3];
+    rep->grid_cap = cfg[4];
+    rep->candidates = tried;
+    rep->default_ms = def_ms;
+    rep->best_ms = best;
+  }
   return RP_OK;
 }
 

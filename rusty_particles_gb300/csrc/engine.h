@@ -20,6 +20,7 @@ struct HostParticle {
   double r, m;
   uint8_t fixed;
   uint32_t tag;
+  uint32_t group;  // independent bed (0 unless set)
 };
 
 struct Totals {
@@ -47,7 +48,16 @@ class Engine {
   int force_path = 0;  // 0 contact-parallel, 1 one thread per particle
 
   int add_particle(const double x[3], double r, double m, int fixed);
-  int add_triangles(size_t n, const float* v, const float* nrm);
+  int add_triangles(size_t n, const float* v, const float* nrm, uint32_t group = GROUP_ALL,
+                    const WallMotion* motion = nullptr);
+  // groups: independent beds stepped together
+  int set_particle_groups(size_t n, const uint32_t* groups);
+  int get_particle_groups(size_t n, uint32_t* groups);
+  int set_group_material(uint32_t group, const Material& m);
+  Law make_law(const Material& m) const;
+  // launch shapes of the force pass (0 = default) and their autotuner
+  int bs_filter = 0, bs_force = 0, bs_accum = 0, grid_cap = 0;
+  int autotune(rp_tune_report* rep);
   int enable_gpu(int device);
   int step(uint64_t n);
   size_t count();
@@ -80,6 +90,13 @@ class Engine {
   bool host_valid_ = true, dev_valid_ = false;
   uint32_t next_tag_ = 0;
   std::vector<float> tri_v_, tri_n_;
+  std::vector<uint32_t> tri_group_;  // per triangle (GROUP_ALL unless given)
+  std::vector<uint32_t> tri_motion_;  // per triangle (NO_MOTION unless given)
+  std::vector<WallMotion> motions_;
+  WallMotion* motions_d_ = nullptr;
+  std::vector<Material> gmat_;       // per group (index 0 unused: the particle material)
+  std::vector<uint8_t> gmat_set_;
+  Law* glaw_d_ = nullptr;
   double ms_total_ = 0.0;
   uint64_t launches_ = 0;
   uint64_t force_launches_ = 0;
@@ -133,6 +150,8 @@ class Engine {
   float* jguess_ = nullptr;
   uint32_t *nnet_ = nullptr, *noff_ = nullptr;
   size_t jq_alloc_ = 0;
+  uint32_t* jfb_ = nullptr;  // pairs deferred to the reference-Newton pass
+  size_t jfb_alloc_ = 0;
   int ensure_jkr_buffers();
   int step_kernels_ = 4;  // kernels of one device-loop step outside the rebuild chain
   TriRec* tri_d_ = nullptr;

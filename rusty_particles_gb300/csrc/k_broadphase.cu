@@ -291,6 +291,7 @@ __global__ void k_reorder(StepParams P, const uint32_t* perm) {
     D.tag[k] = S.tag[o];
     D.xref[k] = make_float4((float)x.x, (float)x.y, (float)x.z, 0.f);
     D.xf[k] = S.xf[o];
+    if (P.ngroups > 1) D.grp[k] = S.grp[o];
   }
 }
 
@@ -317,6 +318,7 @@ __global__ void k_build_nlist(StepParams P, const uint32_t* cstart, const uint32
     const D4 xi = B.xr[k];
     const float4 xif = B.xf[k];
     const float ri = xif.w;
+    const uint32_t gk = P.ngroups > 1 ? B.grp[k] : 0u;  // particles of other groups never interact
     const float Xi = fmaxf(fmaxf(fabsf(xif.x), fabsf(xif.y)), fabsf(xif.z));
     uint32_t cl = fine_cell(P, xi.x, xi.y, xi.z);
     int c[3];
@@ -354,6 +356,7 @@ __global__ void k_build_nlist(StepParams P, const uint32_t* cstart, const uint32
           uint32_t e = cend[cell];
           for (uint32_t j = s; j < e; ++j) {
             if ((int)j == k) continue;
+            if (P.ngroups > 1 && B.grp[j] != gk) continue;
             // FP32 on the position mirror: each difference is within
             // 2^-24 (2X + |d| + L) of the exact one, so growing the radius by
             // 2.5e-7 (2X + L) + a relative 1e-5 keeps the list a superset

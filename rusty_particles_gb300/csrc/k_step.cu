@@ -119,11 +119,11 @@ __device__ __forceinline__ R jkr_mag(R overlap, R es, R rs, R gamma, bool* near 
 // step, and turned into the reference's force 4 E* a^3/(3 R*) - sqrt(8 pi
 // gamma E* a^3) = E* a (4 a^2/(3 R*) - sqrt(C a)). The pull-off cut is decided
 // in FP64 and left to the reference's loop when within 1e-7 of the terms.
-__device__ __forceinline__ int jkr_learned(const StepParams& P, double overlap, double rs, float guess, double& fm,
-                                           uint32_t& iters) {
+__device__ __forceinline__ int jkr_learned(const StepParams& P, const Law& L, double overlap, double rs, float guess,
+                                           double& fm, uint32_t& iters) {
   const float rsf = (float)rs;
   const float x = (float)overlap / rsf;
-  const float c = P.jkr_Cf / rsf;
+  const float c = L.jkr_Cf / rsf;
   const float c23 = jkr_c23(c);
   const int cls = jkr_certify(x, c, c23, overlap > 0.0);
   if (cls == JKR_ZERO) {
@@ -133,7 +133,7 @@ __device__ __forceinline__ int jkr_learned(const StepParams& P, double overlap, 
   if (cls == JKR_WALK) {
     // the reference's halving walk, then its own tail (src/physics.rs:193-218),
     // operation for operation in FP64
-    const double es = P.es_pp, gamma = P.gamma_pp;
+    const double es = L.es_pp, gamma = L.gamma_pp;
     const double eight_pi = 8.0 * kPi;
     const double c_val = eight_pi * gamma / es;
     double a = sqrt(rs * overlap);
@@ -174,7 +174,7 @@ __device__ __forceinline__ int jkr_learned(const StepParams& P, double overlap, 
   // FP64 residual of a = u R*: sqrt(C a) from the FP32 root plus one Newton
   // step of the square root (error ~1e-14), no FP64 division
   const double ud = (double)u;
-  const double Ca = P.jkr_C * (ud * rs);
+  const double Ca = L.jkr_C * (ud * rs);
   const float s0 = sqrtf((float)Ca);
   if (!(s0 > 0.0f)) return JKR_FALLBACK;
   const double ts = (double)s0 + (Ca - (double)s0 * (double)s0) * (double)(0.5f / s0);
@@ -187,12 +187,12 @@ __device__ __forceinline__ int jkr_learned(const StepParams& P, double overlap, 
   const double u1 = ud - (double)du;
   const float q = du / u;
   const double ts1 = ts * (1.0 - (double)(0.5f * q + 0.125f * q * q));
-  const double es = P.es_pp;
+  const double es = L.es_pp;
   const double a1 = u1 * rs;
   const double term1 = (4.0 / 3.0) * es * (u1 * u1 * u1) * (rs * rs);
   const double term2 = es * a1 * ts1;
   const double fmv = term1 - term2;
-  const double f_pull = (-2.0 / 3.0) * kPi * P.gamma_pp * rs;
+  const double f_pull = (-2.0 / 3.0) * kPi * L.gamma_pp * rs;
   if (fabs(fmv - f_pull) <= 1e-7 * (term1 + term2)) return JKR_FALLBACK;
   fm = fmv < f_pull ? 0.0 : fmv;
   return JKR_CONVERGES;
@@ -277,15 +277,18 @@ __device__ __forceinline__ T3<R> spring_coulomb(R fn, T3<R> rv, T3<R> n, T3<R>& 
 // loading/unloading sign and detachment, JKR's cut-offs) or an sJKR
 // near-cancellation lies within FP32 rounding: the caller then evaluates the
 // pair in FP64, so both forms take the same branches.
-// With P.jkr_solver != 0 the JKR magnitude comes from jkr_learned (`guess` is
-// the network's a/R*, or negative / NaN for none; `tally` counts accepted /
-// zero / fallback and
-// FP32 Newton steps when not null).
+// L holds the material constants of the pair's group. With P.jkr_solver != 0
+// the JKR magnitude comes from jkr_learned (`guess` is the network's a/R*, or
+// negative / NaN for none; `tally` counts accepted / zero / fallback / walk
+// and FP32 Newton steps when not null). A pair that needs the reference's
+// Newton iteration sets *deferred and returns at once, touching nothing, when
+// `deferred` is given; `newton` forces the reference's iteration.
 template <typename R, bool PHYS, bool HIST>
-__device__ __forceinline__ bool pair_contact(const StepParams& P, V d, double d2, double rsum, double ri, double rj,
-                                             double mi, double mj, V vi, V vj, V wi, V wj, double* hist, size_t plane,
-                                             V& fc_out, V& tc_out, V& n_out, bool& excess, float guess = -1.0f,
-                                             uint32_t* tally = nullptr) {
+__device__ __forceinline__ bool pair_contact(const StepParams& P, const Law& L, V d, double d2, double rsum, double ri,
+                                             double rj, double mi, double mj, V vi, V vj, V wi, V wj, double* hist,
+                                             size_t plane, V& fc_out, V& tc_out, V& n_out, bool& excess,
+                                             float guess = -1.0f, uint32_t* tally = nullptr,
+                                             bool* deferred = nullptr, bool newton = false) {
   constexpr bool F32 = sizeof(R) == sizeof(float);
   R overlap;
   T3<R> n;
@@ -326,27 +329,31 @@ __device__ __forceinline__ bool pair_contact(const StepParams& P, V d, double d2
   const R ms = ((R)mi * (R)mj) / ((R)mi + (R)mj);
   R fmag;
   int jkind = JKR_FALLBACK;
-  if (P.nmodel == 3 && P.jkr_solver != 0 && P.gamma_pp > 0.0) {
+  if (P.nmodel == 3 && P.jkr_solver != 0 && !newton && L.gamma_pp > 0.0) {
     double fmd = 0.0;
     uint32_t it = 0;
-    jkind = jkr_learned(P, (double)overlap, (double)rs, guess, fmd, it);
+    jkind = jkr_learned(P, L, (double)overlap, (double)rs, guess, fmd, it);
     if (jkind != JKR_FALLBACK) fmag = (R)fmd;
     if (tally) {
       tally[jkind == JKR_CONVERGES ? 0 : (jkind == JKR_ZERO ? 1 : (jkind == JKR_WALK ? 5 : 2))] += 1;
       tally[4] += it;
     }
+    if (jkind == JKR_FALLBACK && deferred) {
+      *deferred = true;
+      return true;
+    }
   }
   if (jkind != JKR_FALLBACK) {
   } else if (F32 && P.nmodel == 3) {
     bool near = false;
-    fmag = jkr_mag<R>(overlap, (R)P.es_pp, rs, (R)P.gamma_pp, &near);
+    fmag = jkr_mag<R>(overlap, (R)L.es_pp, rs, (R)L.gamma_pp, &near);
     if (near) return false;
   } else {
-    fmag = normal_mag<R>(P.nmodel, overlap, n, rv, (R)P.es_pp, rs, ms, (R)P.beta_abs, (R)P.gamma_pp, false);
+    fmag = normal_mag<R>(P.nmodel, overlap, n, rv, (R)L.es_pp, rs, ms, (R)L.beta_abs, (R)L.gamma_pp, false);
   }
-  if (F32 && P.nmodel == 4 && P.gamma_pp > 0.0) {
+  if (F32 && P.nmodel == 4 && L.gamma_pp > 0.0) {
     const R vn = dot(rv, n);
-    const R gamma = (R)P.gamma_pp, es = (R)P.es_pp;
+    const R gamma = (R)L.gamma_pp, es = (R)L.es_pp;
     const R f_pull = R(1.5) * R(kPi) * gamma * rs;
     const R delta_c = -sqrt(R(3) * (R(kPi) * R(kPi)) * (gamma * gamma) * rs / (es * es));
     if (fabs(vn) <= R(1e-6) * (len(rv) + R(1e-30))) return false;
@@ -363,19 +370,19 @@ __device__ __forceinline__ bool pair_contact(const StepParams& P, V d, double d2
       const R vt2 = dot(vt, vt);
       if (fabs(vt2 - R(1e-8)) <= R(1e-5) * (dot(rv, rv) + R(1e-8))) return false;
     }
-    ft = coulomb_force<R>(fnm, rv, n, (R)P.pm.mu);
+    ft = coulomb_force<R>(fnm, rv, n, (R)L.mu);
   } else if (!PHYS) {
     // G* = 0 (src/material.rs:39-50): the spring force is +-0, or NaN when
     // Mindlin takes sqrt of a negative overlap.
-    R kt = P.tmodel == 2 ? R(8) * (R)P.gs_pp * sqrt(rs * overlap) : (R)P.gs_pp * rs;
+    R kt = P.tmodel == 2 ? R(8) * (R)L.gs_pp * sqrt(rs * overlap) : (R)L.gs_pp * rs;
     ft = (kt != kt) ? t3(kt, kt, kt) : t3(R(0), R(0), R(0));
   } else {
     T3<R> xi_s = t3(R(0), R(0), R(0));
     if (overlap > R(0)) {
-      R kt = P.tmodel == 2 ? R(8) * (R)P.gs_pp * sqrt(rs * overlap) : (R)P.gs_pp * rs;
+      R kt = P.tmodel == 2 ? R(8) * (R)L.gs_pp * sqrt(rs * overlap) : (R)L.gs_pp * rs;
       if (HIST) xi_s = t3((R)hist[0], (R)hist[plane], (R)hist[2 * plane]);
       xi_s = xi_s - dot(xi_s, n) * n;
-      ft = spring_coulomb<R>(fnm, rv, n, xi_s, kt, (R)P.pm.mu, (R)P.dt);
+      ft = spring_coulomb<R>(fnm, rv, n, xi_s, kt, (R)L.mu, (R)P.dt);
     } else {
       ft = t3(R(0), R(0), R(0));
     }
@@ -535,8 +542,9 @@ __global__ void __launch_bounds__(256) k_second_half(StepParams P) {
 // triangle's box by a margin covering the FP32 error), and a triangle whose
 // plane is farther than the radius (plus rounding) cannot touch the sphere,
 // because the closest point lies in that plane: both skip FP64 work only.
-__device__ __forceinline__ void wall_forces(const StepParams& P, V xi, float4 xf, V vi, V wi, double ri, double mi,
-                                            double beta_abs, V& F, V& T, bool& excess) {
+// Triangles of another group than the particle's (gi) are not walls for it.
+__device__ __forceinline__ void wall_forces(const StepParams& P, const Law& L, uint32_t gi, V xi, float4 xf, V vi,
+                                            V wi, double ri, double mi, V& F, V& T, bool& excess) {
   if (P.ntri > 0) {
     const float q0 = floorf((xf.x - P.tminf[0]) * P.tinvf);
     const float q1 = floorf((xf.y - P.tminf[1]) * P.tinvf);
@@ -549,6 +557,7 @@ __device__ __forceinline__ void wall_forces(const StepParams& P, V xi, float4 xf
       const float xmag = fmaxf(fmaxf(fabsf(xf.x), fabsf(xf.y)), fabsf(xf.z));
       for (uint32_t t = s; t < e; ++t) {
         const TriRec& tr = P.tri[P.titems[t]];
+        if (tr.group != GROUP_ALL && tr.group != gi) continue;
         // FP32 rounding of n, n.v0 and x moves n.x - n.v0 by at most
         // ~3e-7 (|x| + |n.v0|) + 1.1e-7 |x - v0|; the margin is larger
         const float4 pl = tr.plane;
@@ -612,9 +621,14 @@ __device__ __forceinline__ void wall_forces(const StepParams& P, V xi, float4 xf
         const V n = dist > 1e-6 ? dv / dist : vmk(tr.n[0], tr.n[1], tr.n[2]);
         if (pen > 0.2 * ri) excess = true;
         const V ra = (-n) * ri;
-        const V rv = vi + cross(wi, ra);
-        const V fnv = normal_force<double>(P.nmodel, pen, n, rv, P.es_pw, ri, mi, beta_abs, P.gamma_pw, true);
-        const V fc = fnv + coulomb_force<double>(len(fnv), rv, n, P.pm.mu);
+        V rv = vi + cross(wi, ra);
+        if (tr.motion != NO_MOTION) {  // a moving wall: relative to its surface velocity at the contact point
+          const WallMotion& M = P.motions[tr.motion];
+          const V vw = vmk(M.v[0], M.v[1], M.v[2]) + cross(vmk(M.w[0], M.w[1], M.w[2]), cp - vmk(M.c[0], M.c[1], M.c[2]));
+          rv = rv - vw;
+        }
+        const V fnv = normal_force<double>(P.nmodel, pen, n, rv, L.es_pw, ri, mi, L.beta_abs, L.gamma_pw, true);
+        const V fc = fnv + coulomb_force<double>(len(fnv), rv, n, L.mu);
         F = F + fc;
         T = T + cross(ra, fc);
       }
@@ -634,12 +648,13 @@ __global__ void __launch_bounds__(128) k_force(StepParams P) {
   if (C->halt) return;
   const Bank B = P.bank[C->bank];
   const bool adh = (P.nmodel == 3 || P.nmodel == 4);
-  const double beta_abs = P.beta_abs;
   const size_t plane = (size_t)P.n * P.cap;
   bool excess = false;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < P.n; k += gridDim.x * blockDim.x) {
     const uint32_t fl = B.flags[k];
     if (fl & PF_DEAD) continue;
+    const Law lw = law_of(P, B, k);
+    const uint32_t gi = P.ngroups > 1 ? B.grp[k] : 0u;
     const D4 xi4 = B.xr[k], vi4 = B.vm[k], wi4 = B.wc[k];
     const V xi = xyz(xi4), vi = xyz(vi4), wi = xyz(wi4);
     const double ri = xi4.w, mi = vi4.w;
@@ -697,9 +712,9 @@ __global__ void __launch_bounds__(128) k_force(StepParams P) {
         if (visits > 0) {
           const D4 vj4 = B.vm[j];
           V fc, tc, nrm;
-          if (!pair_contact<R, PHYS, HIST>(P, d, d2, rsum, ri, rj, mi, vj4.w, vi, xyz(vj4), wi, xyz(wj4),
+          if (!pair_contact<R, PHYS, HIST>(P, lw, d, d2, rsum, ri, rj, mi, vj4.w, vi, xyz(vj4), wi, xyz(wj4),
                                            HIST ? B.hist + hi : nullptr, plane, fc, tc, nrm, excess))
-            pair_contact<double, PHYS, HIST>(P, d, d2, rsum, ri, rj, mi, vj4.w, vi, xyz(vj4), wi, xyz(wj4),
+            pair_contact<double, PHYS, HIST>(P, lw, d, d2, rsum, ri, rj, mi, vj4.w, vi, xyz(vj4), wi, xyz(wj4),
                                              HIST ? B.hist + hi : nullptr, plane, fc, tc, nrm, excess);
           for (int t = 0; t < visits; ++t) {
             F = F + fc;
@@ -714,7 +729,7 @@ __global__ void __launch_bounds__(128) k_force(StepParams P) {
       }
       if (P.debug) P.dbgMult[hi] = (uint8_t)visits;
     }
-    wall_forces(P, xi, xif, vi, wi, ri, mi, beta_abs, F, T, excess);
+    wall_forces(P, lw, gi, xi, xif, vi, wi, ri, mi, F, T, excess);
     if (P.debug) {
       P.dbgF[3 * (size_t)k] = F.x; P.dbgF[3 * (size_t)k + 1] = F.y; P.dbgF[3 * (size_t)k + 2] = F.z;
       P.dbgT[3 * (size_t)k] = T.x; P.dbgT[3 * (size_t)k + 1] = T.y; P.dbgT[3 * (size_t)k + 2] = T.z;
@@ -767,14 +782,14 @@ __device__ __forceinline__ V mic(const StepParams& P, V d) {
 // rounding (~2.4e-7 of the coordinates). A queued pair the exact test rejects
 // only wastes a network row; a converging pair without a row falls back to the
 // reference's Newton.
-__device__ __forceinline__ bool jkr_net_hint(const StepParams& P, float4 xif, float4 xjf) {
+__device__ __forceinline__ bool jkr_net_hint(const StepParams& P, float Cf, float4 xif, float4 xjf) {
   float fx = xif.x - xjf.x, fy = xif.y - xjf.y, fz = xif.z - xjf.z;
   if (P.periodic[0]) { const float L = (float)P.bsize[0]; if (fx > 0.5f * L) fx -= L; else if (fx < -0.5f * L) fx += L; }
   if (P.periodic[1]) { const float L = (float)P.bsize[1]; if (fy > 0.5f * L) fy -= L; else if (fy < -0.5f * L) fy += L; }
   if (P.periodic[2]) { const float L = (float)P.bsize[2]; if (fz > 0.5f * L) fz -= L; else if (fz < -0.5f * L) fz += L; }
   const float rsum = xif.w + xjf.w;
   const float rs = xif.w * xjf.w / rsum;
-  const float c = P.jkr_Cf / rs;
+  const float c = Cf / rs;
   if (!(c >= kJkrCMin && c <= kJkrCMax)) return false;
   const float c23 = jkr_c23(c);
   const float x = (rsum - sqrtf(fx * fx + fy * fy + fz * fz)) / rs;
@@ -795,14 +810,14 @@ __device__ __forceinline__ bool jkr_net_hint(const StepParams& P, float4 xif, fl
 // JKR force is exactly zero), decided on the FP32 position mirror with that
 // mirror's rounding added to the certificate's margin. Symmetric in (i, j)
 // bit for bit, so both ends of a pair drop it or keep it together.
-__device__ __forceinline__ bool jkr_far_zero(const StepParams& P, float4 xif, float Xi, float4 xjf) {
+__device__ __forceinline__ bool jkr_far_zero(const StepParams& P, float Cf, float4 xif, float Xi, float4 xjf) {
   float fx = xif.x - xjf.x, fy = xif.y - xjf.y, fz = xif.z - xjf.z;
   if (P.periodic[0]) { const float L = (float)P.bsize[0]; if (fx > 0.5f * L) fx -= L; else if (fx < -0.5f * L) fx += L; }
   if (P.periodic[1]) { const float L = (float)P.bsize[1]; if (fy > 0.5f * L) fy -= L; else if (fy < -0.5f * L) fy += L; }
   if (P.periodic[2]) { const float L = (float)P.bsize[2]; if (fz > 0.5f * L) fz -= L; else if (fz < -0.5f * L) fz += L; }
   const float rsum = xif.w + xjf.w;
   const float rs = (xif.w * xjf.w) / rsum;
-  const float c = P.jkr_Cf / rs;
+  const float c = Cf / rs;
   if (!(c > 0.0f && c < 1e30f)) return false;
   const float c23 = jkr_c23(c);
   const float d = sqrtf(fx * fx + fy * fy + fz * fz);
@@ -821,24 +836,26 @@ __device__ __forceinline__ bool jkr_far_zero(const StepParams& P, float4 xif, fl
 // seen from both ends, or the only end that sees it). The pretest is
 // symmetric, so a pair seen from both ends is a candidate at both.
 template <bool PHYS, bool HIST>
-__global__ void __launch_bounds__(128) k_contact_filter(StepParams P) {
+__global__ void __launch_bounds__(256) k_contact_filter(StepParams P) {
   Ctrl* C = P.ctrl;
   if (C->halt) return;
   const Bank B = P.bank[C->bank];
   const bool adh = (P.nmodel == 3 || P.nmodel == 4);
-  const bool learn = P.jkr_solver == 1 && P.nmodel == 3 && P.gamma_pp > 0.0 && P.mlp != nullptr;
+  const bool learn_any = P.jkr_solver == 1 && P.nmodel == 3 && P.mlp != nullptr;
   // Certified-zero JKR pairs add exactly +-0 to F and T when the tangential
   // force then vanishes too (Coulomb with |F_n| = 0; physical-mode springs
   // reset out of contact): with the certified solvers they are not
   // candidates at all. Parity-mode springs (G* = 0, NaN for Mindlin at
   // negative overlap) and debug recording keep every pair.
-  const bool zdrop = P.jkr_solver != 0 && P.nmodel == 3 && P.gamma_pp > 0.0 && P.pretest && !P.debug &&
-                     (P.tmodel == 0 || PHYS);
+  const bool zdrop_any = P.jkr_solver != 0 && P.nmodel == 3 && P.pretest && !P.debug && (P.tmodel == 0 || PHYS);
   const size_t plane = (size_t)P.n * P.cap;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < P.n; k += gridDim.x * blockDim.x) {
     uint32_t nrec = 0, ncmp = 0, nnet = 0;
     if (!(B.flags[k] & PF_DEAD)) {
       const unsigned long long ci = PHYS ? 0ull : (unsigned long long)__double_as_longlong(B.wc[k].w);
+      const Law lw = law_of(P, B, k);  // pairs never cross groups (the lists exclude them)
+      const bool adhesive = lw.gamma_pp > 0.0;
+      const bool learn = learn_any && adhesive, zdrop = zdrop_any && adhesive;
       const float4 xif = B.xf[k];
       const float Xi = fmaxf(fmaxf(fabsf(xif.x), fabsf(xif.y)), fabsf(xif.z));
       const uint32_t cnt = B.ncnt[k];
@@ -849,7 +866,7 @@ __global__ void __launch_bounds__(128) k_contact_filter(StepParams P) {
         const size_t hi = (size_t)k * P.cap + m;
         int vij = 0, vji = 0;
         const float4 xjf = B.xf[j];
-        if (!(P.pretest && pretest_far(P, xif, Xi, xjf, adh)) && !(zdrop && jkr_far_zero(P, xif, Xi, xjf))) {
+        if (!(P.pretest && pretest_far(P, xif, Xi, xjf, adh)) && !(zdrop && jkr_far_zero(P, lw.jkr_Cf, xif, Xi, xjf))) {
           if (PHYS) {
             vij = vji = 1;
           } else {
@@ -860,7 +877,7 @@ __global__ void __launch_bounds__(128) k_contact_filter(StepParams P) {
         }
         if (vij > 0) {
           const bool evaluates = !(vji > 0 && (uint32_t)k > j);
-          const uint32_t net = (learn && evaluates && jkr_net_hint(P, xif, xjf)) ? CREC_NET : 0u;
+          const uint32_t net = (learn && evaluates && jkr_net_hint(P, lw.jkr_Cf, xif, xjf)) ? CREC_NET : 0u;
           out[nrec] = CRec{j, m | ((uint32_t)vij << 16) | ((uint32_t)vji << 24) | net};
           ++nrec;
           if (evaluates) ++ncmp;
@@ -877,7 +894,7 @@ __global__ void __launch_bounds__(128) k_contact_filter(StepParams P) {
     }
     P.ccnt[k] = nrec;
     P.ncomp[k] = ncmp;
-    if (learn) P.nnet[k] = nnet;
+    if (learn_any) P.nnet[k] = nnet;
   }
 }
 
@@ -885,7 +902,8 @@ __global__ void __launch_bounds__(128) k_contact_filter(StepParams P) {
 // particle order, at the offsets of the scan of the per-particle counts).
 __global__ void __launch_bounds__(256) k_contact_index(StepParams P) {
   if (P.ctrl->halt) return;
-  const bool learn = P.jkr_solver == 1 && P.nmodel == 3 && P.gamma_pp > 0.0 && P.mlp != nullptr;
+  const bool learn = P.jkr_solver == 1 && P.nmodel == 3 && P.mlp != nullptr;
+  if (blockIdx.x == 0 && threadIdx.x == 0) P.ctot[3] = 0u;  // deferred pairs of this step
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < P.n; k += gridDim.x * blockDim.x) {
     const uint32_t n = P.ccnt[k];
     uint32_t q = P.poff[k];
@@ -921,8 +939,6 @@ __global__ void __launch_bounds__(128) k_jkr_mlp(StepParams P) {
   const Bank B = P.bank[C->bank];
   const int lane = threadIdx.x & 31;
   const uint32_t stride = gridDim.x * blockDim.x;
-  const float es = (float)P.es_pp, gam = (float)P.gamma_pp;
-  const float les = logf(es), lgam = logf(gam);
   for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < qn; base += stride) {
     const uint32_t idx = base + lane;
     const bool valid = idx < qn;
@@ -941,12 +957,13 @@ __global__ void __launch_bounds__(128) k_jkr_mlp(StepParams P) {
       const double d2 = dot(d, d);
       const double rsum = xi4.w + xj4.w;
       const float ov = (float)(rsum * rsum - d2) / ((float)rsum + sqrtf((float)d2));
-      const float rs = (float)(xi4.w * xj4.w / rsum);
+      const float rs = ((float)xi4.w * (float)xj4.w) / (float)rsum;  // a feature: FP32 is enough
       const float x = ov / rs;
-      const float c = P.jkr_Cf / rs;
+      const Law lw = law_of(P, B, (int)k);
+      const float c = lw.jkr_Cf / rs;
       const float c23 = jkr_c23(c);
-      // the features of jkr_raw_features, with ln E* and ln gamma hoisted
-      const float raw[4] = {jkr_overlap_feature(x, c23), logf(rs), les, lgam};
+      float raw[4];
+      jkr_raw_features(x, c23, rs, (float)lw.es_pp, (float)lw.gamma_pp, raw);
       ok = true;
 #pragma unroll
       for (int a = 0; a < 4; ++a) {
@@ -967,75 +984,106 @@ __global__ void __launch_bounds__(128) k_jkr_mlp(StepParams P) {
 // evaluated from that end it gives -f bit for bit) times its own visit count,
 // with its own torque (n r_j) x (-f), and in physical mode the negated spring.
 // A candidate outside the cutoff gives zero results at both ends.
+//
+// With a certified JKR solver in FP64, a pair whose JKR force needs the
+// reference's own Newton iteration (up to 20 FP64 steps) is not evaluated in
+// this pass: it would hold its whole warp for those steps. It is appended to
+// a deferred list (contact_eval returns true) and k_contact_deferred
+// evaluates the deferred pairs densely; each pair writes the same result slots
+// in either pass, so the outcome does not depend on the order.
 template <bool PHYS, bool HIST, typename R>
-__global__ void __launch_bounds__(128) k_contact_force(StepParams P) {
+__device__ __forceinline__ bool contact_eval(const StepParams& P, const Bank& B, uint32_t t, bool first_pass,
+                                             bool& excess, uint32_t* tally) {
+  const size_t plane = (size_t)P.n * P.cap;
+  const bool adh = (P.nmodel == 3 || P.nmodel == 4);
+  const uint32_t s = P.clist[t];
+  const uint32_t k = s / (uint32_t)P.cap, c = s - k * (uint32_t)P.cap;
+  const CRec r = P.crec[s];
+  const uint32_t j = r.j, m = r.mv & 0xFFFFu;
+  const int vij = (r.mv >> 16) & 0xFF, vji = crec_vji(r.mv);
+  const float guess = (first_pass && (r.mv & CREC_NET)) ? P.jguess[t] : -1.0f;
+  if (tally && (r.mv & CREC_NET)) tally[3] += 1;
+  const D4 xi4 = B.xr[k], xj4 = B.xr[j];
+  const V d = mic(P, xyz(xi4) - xyz(xj4));
+  const double d2 = dot(d, d);
+  const double rsum = xi4.w + xj4.w;
+  const double cut = rsum + (adh ? rsum * 0.5 : 0.0);
+  const bool in = d2 < cut * cut;
+  const size_t hik = (size_t)k * P.cap + m;
+  double* hk = HIST ? B.hist + hik : nullptr;
+  V fc = vmk(0.0, 0.0, 0.0), tc = fc, nrm = fc;
+  if (in) {
+    const D4 vi4 = B.vm[k], wi4 = B.wc[k], vj4 = B.vm[j], wj4 = B.wc[j];
+    const Law lw = law_of(P, B, (int)k);
+    bool deferred = false;
+    const bool can_defer = first_pass && sizeof(R) == sizeof(double) && P.jfb != nullptr;
+    if (!pair_contact<R, PHYS, HIST>(P, lw, d, d2, rsum, xi4.w, xj4.w, vi4.w, vj4.w, xyz(vi4), xyz(vj4), xyz(wi4),
+                                     xyz(wj4), hk, plane, fc, tc, nrm, excess, guess, tally,
+                                     can_defer ? &deferred : nullptr, !first_pass))
+      pair_contact<double, PHYS, HIST>(P, lw, d, d2, rsum, xi4.w, xj4.w, vi4.w, vj4.w, xyz(vi4), xyz(vj4),
+                                       xyz(wi4), xyz(wj4), hk, plane, fc, tc, nrm, excess, guess, nullptr, nullptr,
+                                       !first_pass);
+    if (deferred) return true;
+  } else if (HIST) {
+    hk[0] = 0.0;
+    hk[plane] = 0.0;
+    hk[2 * plane] = 0.0;
+  }
+  if (P.debug) P.dbgMult[hik] = (uint8_t)(in ? vij : 0);
+  double* out = P.cres + 6 * (size_t)(P.coff[k] + c);
+  const double sv = (double)vij;
+  out[0] = fc.x * sv; out[1] = fc.y * sv; out[2] = fc.z * sv;
+  out[3] = tc.x * sv; out[4] = tc.y * sv; out[5] = tc.z * sv;
+  if (vji > 0) {
+    const uint32_t nj = P.ccnt[j];
+    const CRec* rj = P.crec + (size_t)j * P.cap;
+    for (uint32_t c2 = 0; c2 < nj; ++c2) {
+      if (rj[c2].j != k) continue;
+      const V f2 = -fc;
+      V t2;
+      if (sizeof(R) == sizeof(float)) {
+        const Vf raj = cvt<float>(nrm) * (float)xj4.w;
+        t2 = cvt<double>(cross(raj, cvt<float>(f2)));
+      } else {
+        t2 = cross(nrm * xj4.w, f2);
+      }
+      double* o2 = P.cres + 6 * (size_t)(P.coff[j] + c2);
+      const double s2 = (double)vji;
+      o2[0] = f2.x * s2; o2[1] = f2.y * s2; o2[2] = f2.z * s2;
+      o2[3] = t2.x * s2; o2[4] = t2.y * s2; o2[5] = t2.z * s2;
+      const size_t h2 = (size_t)j * P.cap + (rj[c2].mv & 0xFFFFu);
+      if (HIST) {
+        B.hist[h2] = -hk[0];
+        B.hist[plane + h2] = -hk[plane];
+        B.hist[2 * plane + h2] = -hk[2 * plane];
+      }
+      if (P.debug) P.dbgMult[h2] = (uint8_t)(in ? vji : 0);
+      break;
+    }
+  }
+  return false;
+}
+
+template <bool PHYS, bool HIST, typename R>
+__global__ void __launch_bounds__(256) k_contact_force(StepParams P) {
   Ctrl* C = P.ctrl;
   if (C->halt) return;
   const Bank B = P.bank[C->bank];
-  const size_t plane = (size_t)P.n * P.cap;
   const uint32_t total = P.ctot[1];
-  const bool adh = (P.nmodel == 3 || P.nmodel == 4);
   bool excess = false;
   uint32_t tally[6] = {0u, 0u, 0u, 0u, 0u, 0u};
+  const int lane = threadIdx.x & 31;
   for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
-    const uint32_t s = P.clist[t];
-    const uint32_t k = s / (uint32_t)P.cap, c = s - k * (uint32_t)P.cap;
-    const CRec r = P.crec[s];
-    const uint32_t j = r.j, m = r.mv & 0xFFFFu;
-    const int vij = (r.mv >> 16) & 0xFF, vji = crec_vji(r.mv);
-    const float guess = (r.mv & CREC_NET) ? P.jguess[t] : -1.0f;
-    if (r.mv & CREC_NET) tally[3] += 1;
-    const D4 xi4 = B.xr[k], xj4 = B.xr[j];
-    const V d = mic(P, xyz(xi4) - xyz(xj4));
-    const double d2 = dot(d, d);
-    const double rsum = xi4.w + xj4.w;
-    const double cut = rsum + (adh ? rsum * 0.5 : 0.0);
-    const bool in = d2 < cut * cut;
-    const size_t hik = (size_t)k * P.cap + m;
-    double* hk = HIST ? B.hist + hik : nullptr;
-    V fc = vmk(0.0, 0.0, 0.0), tc = fc, nrm = fc;
-    if (in) {
-      const D4 vi4 = B.vm[k], wi4 = B.wc[k], vj4 = B.vm[j], wj4 = B.wc[j];
-      if (!pair_contact<R, PHYS, HIST>(P, d, d2, rsum, xi4.w, xj4.w, vi4.w, vj4.w, xyz(vi4), xyz(vj4), xyz(wi4),
-                                       xyz(wj4), hk, plane, fc, tc, nrm, excess, guess, tally))
-        pair_contact<double, PHYS, HIST>(P, d, d2, rsum, xi4.w, xj4.w, vi4.w, vj4.w, xyz(vi4), xyz(vj4), xyz(wi4),
-                                         xyz(wj4), hk, plane, fc, tc, nrm, excess, guess);
-    } else if (HIST) {
-      hk[0] = 0.0;
-      hk[plane] = 0.0;
-      hk[2 * plane] = 0.0;
-    }
-    if (P.debug) P.dbgMult[hik] = (uint8_t)(in ? vij : 0);
-    double* out = P.cres + 6 * (size_t)(P.coff[k] + c);
-    const double sv = (double)vij;
-    out[0] = fc.x * sv; out[1] = fc.y * sv; out[2] = fc.z * sv;
-    out[3] = tc.x * sv; out[4] = tc.y * sv; out[5] = tc.z * sv;
-    if (vji > 0) {
-      const uint32_t nj = P.ccnt[j];
-      const CRec* rj = P.crec + (size_t)j * P.cap;
-      for (uint32_t c2 = 0; c2 < nj; ++c2) {
-        if (rj[c2].j != k) continue;
-        const V f2 = -fc;
-        V t2;
-        if (sizeof(R) == sizeof(float)) {
-          const Vf raj = cvt<float>(nrm) * (float)xj4.w;
-          t2 = cvt<double>(cross(raj, cvt<float>(f2)));
-        } else {
-          t2 = cross(nrm * xj4.w, f2);
-        }
-        double* o2 = P.cres + 6 * (size_t)(P.coff[j] + c2);
-        const double s2 = (double)vji;
-        o2[0] = f2.x * s2; o2[1] = f2.y * s2; o2[2] = f2.z * s2;
-        o2[3] = t2.x * s2; o2[4] = t2.y * s2; o2[5] = t2.z * s2;
-        const size_t h2 = (size_t)j * P.cap + (rj[c2].mv & 0xFFFFu);
-        if (HIST) {
-          B.hist[h2] = -hk[0];
-          B.hist[plane + h2] = -hk[plane];
-          B.hist[2 * plane + h2] = -hk[2 * plane];
-        }
-        if (P.debug) P.dbgMult[h2] = (uint8_t)(in ? vji : 0);
-        break;
-      }
+    const bool deferred = contact_eval<PHYS, HIST, R>(P, B, t, true, excess, tally);
+    // append the deferred pairs with one atomic per warp
+    const unsigned act = __activemask();
+    const unsigned bal = __ballot_sync(act, deferred);
+    if (bal) {
+      const int leader = __ffs(bal) - 1;
+      uint32_t base = 0;
+      if (lane == leader) base = atomicAdd(P.ctot + 3, (uint32_t)__popc(bal));
+      base = __shfl_sync(act, base, leader);
+      if (deferred) P.jfb[base + (uint32_t)__popc(bal & ((1u << lane) - 1u))] = t;
     }
   }
   if (excess) C->overlap_flag = 1;
@@ -1049,9 +1097,23 @@ __global__ void __launch_bounds__(128) k_contact_force(StepParams P) {
   }
 }
 
+// The deferred pairs of k_contact_force, one thread each, with the
+// reference's Newton iteration for their JKR force.
+template <bool PHYS, bool HIST, typename R>
+__global__ void __launch_bounds__(128) k_contact_deferred(StepParams P) {
+  Ctrl* C = P.ctrl;
+  if (C->halt) return;
+  const Bank B = P.bank[C->bank];
+  const uint32_t total = P.ctot[3];
+  bool excess = false;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x)
+    contact_eval<PHYS, HIST, R>(P, B, P.jfb[i], false, excess, nullptr);
+  if (excess) C->overlap_flag = 1;
+}
+
 // Pass 4: per particle, the contact results in list order, the walls, then
 // a = g + F/m and tau = T (src/simulation.rs:265-271, 532-536).
-__global__ void __launch_bounds__(128) k_accumulate(StepParams P) {
+__global__ void __launch_bounds__(256) k_accumulate(StepParams P) {
   Ctrl* C = P.ctrl;
   if (C->halt) return;
   const Bank B = P.bank[C->bank];
@@ -1067,7 +1129,9 @@ __global__ void __launch_bounds__(128) k_accumulate(StepParams P) {
     }
     const D4 xi4 = B.xr[k], vi4 = B.vm[k], wi4 = B.wc[k];
     const double mi = vi4.w;
-    if (P.ntri > 0) wall_forces(P, xyz(xi4), B.xf[k], xyz(vi4), xyz(wi4), xi4.w, mi, P.beta_abs, F, T, excess);
+    if (P.ntri > 0)
+      wall_forces(P, law_of(P, B, k), P.ngroups > 1 ? B.grp[k] : 0u, xyz(xi4), B.xf[k], xyz(vi4), xyz(wi4), xi4.w,
+                  mi, F, T, excess);
     if (P.debug) {
       P.dbgF[3 * (size_t)k] = F.x; P.dbgF[3 * (size_t)k + 1] = F.y; P.dbgF[3 * (size_t)k + 2] = F.z;
       P.dbgT[3 * (size_t)k] = T.x; P.dbgT[3 * (size_t)k + 1] = T.y; P.dbgT[3 * (size_t)k + 2] = T.z;
@@ -1151,16 +1215,26 @@ static void launch_force_t(const StepParams& P, int g, cudaStream_t s) {
   else k_force<true, false, R><<<g, 128, 0, s>>>(P);
 }
 
+// Grid for a grid-stride kernel of block `bs` over n items, at most `cap` blocks.
+static int shaped_grid(uint64_t n, int bs, int cap) {
+  uint64_t g = (n + (uint64_t)bs - 1) / (uint64_t)bs;
+  if (g < 1) g = 1;
+  if (g > (uint64_t)cap) g = (uint64_t)cap;
+  return (int)g;
+}
+
 template <typename R>
 static int launch_contact_path(const StepParams& P, cudaStream_t s) {
-  const int g = grid_for(P.n, 128);
+  const int bf = P.bs_filter > 0 ? P.bs_filter : 128, bc = P.bs_force > 0 ? P.bs_force : 128,
+            ba = P.bs_accum > 0 ? P.bs_accum : 128, cap = P.grid_cap > 0 ? P.grid_cap : 152 * 64;
+  const int g = shaped_grid((uint64_t)P.n, bf, cap);
   const bool hist = P.mode == 1 && P.tmodel != 0;
-  if (P.mode == 0) k_contact_filter<false, false><<<g, 128, 0, s>>>(P);
-  else if (hist) k_contact_filter<true, true><<<g, 128, 0, s>>>(P);
-  else k_contact_filter<true, false><<<g, 128, 0, s>>>(P);
+  if (P.mode == 0) k_contact_filter<false, false><<<g, bf, 0, s>>>(P);
+  else if (hist) k_contact_filter<true, true><<<g, bf, 0, s>>>(P);
+  else k_contact_filter<true, false><<<g, bf, 0, s>>>(P);
   launch_exclusive_scan(nullptr, P.ccnt, P.coff, (uint32_t)P.n, P.cpart, P.ctot, s);
   launch_exclusive_scan(nullptr, P.ncomp, P.poff, (uint32_t)P.n, P.cpart, P.ctot + 1, s);
-  const bool learn = P.jkr_solver == 1 && P.nmodel == 3 && P.gamma_pp > 0.0 && P.mlp != nullptr;
+  const bool learn = P.jkr_solver == 1 && P.nmodel == 3 && P.mlp != nullptr;
   int launched = 10;
   if (learn) {
     launch_exclusive_scan(nullptr, P.nnet, P.noff, (uint32_t)P.n, P.cpart, P.ctot + 2, s);
@@ -1171,11 +1245,17 @@ static int launch_contact_path(const StepParams& P, cudaStream_t s) {
     k_jkr_mlp<<<152 * 4, 128, 0, s>>>(P);
     ++launched;
   }
-  const int gc = grid_for((uint64_t)P.n * 4, 128);
-  if (P.mode == 0) k_contact_force<false, false, R><<<gc, 128, 0, s>>>(P);
-  else if (hist) k_contact_force<true, true, R><<<gc, 128, 0, s>>>(P);
-  else k_contact_force<true, false, R><<<gc, 128, 0, s>>>(P);
-  k_accumulate<<<g, 128, 0, s>>>(P);
+  const int gc = shaped_grid((uint64_t)P.n * 4, bc, cap);
+  if (P.mode == 0) k_contact_force<false, false, R><<<gc, bc, 0, s>>>(P);
+  else if (hist) k_contact_force<true, true, R><<<gc, bc, 0, s>>>(P);
+  else k_contact_force<true, false, R><<<gc, bc, 0, s>>>(P);
+  if (P.jfb != nullptr && sizeof(R) == sizeof(double)) {
+    if (P.mode == 0) k_contact_deferred<false, false, R><<<152 * 8, 128, 0, s>>>(P);
+    else if (hist) k_contact_deferred<true, true, R><<<152 * 8, 128, 0, s>>>(P);
+    else k_contact_deferred<true, false, R><<<152 * 8, 128, 0, s>>>(P);
+    ++launched;
+  }
+  k_accumulate<<<shaped_grid((uint64_t)P.n, ba, cap), ba, 0, s>>>(P);
   return launched;
 }
 

@@ -260,6 +260,71 @@ int rp_add_mesh_triangles(rp_sim* s, size_t n_triangles, const float* vertices, 
   return s->e->add_triangles(n_triangles, vertices, normals);
 }
 
+int rp_add_mesh_triangles_group(rp_sim* s, size_t n_triangles, const float* vertices, const float* normals,
+                                uint32_t group) {
+  SIM_OR_FAIL(s);
+  if (n_triangles && !vertices) {
+    set_error("null vertex array");
+    return RP_E_INVALID_ARG;
+  }
+  if (group != RP_GROUP_ALL && group >= (1u << 24)) {
+    set_error("group id %u too large (at most 2^24 - 1)", group);
+    return RP_E_INVALID_ARG;
+  }
+  return s->e->add_triangles(n_triangles, vertices, normals, group);
+}
+
+int rp_add_mesh_triangles_moving(rp_sim* s, size_t n_triangles, const float* vertices, const float* normals,
+                                 uint32_t group, const double center[3], const double omega[3],
+                                 const double velocity[3]) {
+  SIM_OR_FAIL(s);
+  if (n_triangles && !vertices) {
+    set_error("null vertex array");
+    return RP_E_INVALID_ARG;
+  }
+  if (!center || !omega || !velocity || !finite3(center) || !finite3(omega) || !finite3(velocity)) {
+    set_error("moving wall needs finite center, omega and velocity");
+    return RP_E_INVALID_ARG;
+  }
+  if (group != RP_GROUP_ALL && group >= (1u << 24)) {
+    set_error("group id %u too large (at most 2^24 - 1)", group);
+    return RP_E_INVALID_ARG;
+  }
+  rp::WallMotion m;
+  for (int k = 0; k < 3; ++k) {
+    m.c[k] = center[k];
+    m.w[k] = omega[k];
+    m.v[k] = velocity[k];
+  }
+  return s->e->add_triangles(n_triangles, vertices, normals, group, &m);
+}
+
+int rp_set_particle_groups(rp_sim* s, size_t n, const uint32_t* groups) {
+  SIM_OR_FAIL(s);
+  if (n && !groups) {
+    set_error("null group array");
+    return RP_E_INVALID_ARG;
+  }
+  return s->e->set_particle_groups(n, groups);
+}
+
+int rp_get_particle_groups(rp_sim* s, size_t n, uint32_t* groups) {
+  SIM_OR_FAIL(s);
+  if (n && !groups) {
+    set_error("null group array");
+    return RP_E_INVALID_ARG;
+  }
+  return s->e->get_particle_groups(n, groups);
+}
+
+int rp_set_group_material(rp_sim* s, uint32_t group, double E, double nu, double rho, double mu, double e,
+                          double gamma) {
+  SIM_OR_FAIL(s);
+  int r = check_material(E, nu, mu, e);
+  if (r != RP_OK) return r;
+  return s->e->set_group_material(group, rp::Material{E, nu, rho, mu, e, gamma});
+}
+
 int rp_set_particle_material(rp_sim* s, double E, double nu, double rho, double mu, double e, double gamma) {
   SIM_OR_FAIL(s);
   int r = check_material(E, nu, mu, e);
@@ -540,6 +605,31 @@ int rp_debug_reference_grid(rp_sim* s, double h, int64_t* cell_of, int64_t* orde
     return RP_E_INVALID_ARG;
   }
   return s->e->debug_reference_grid(h, cell_of, order, n_order, dims);
+}
+
+int rp_autotune(rp_sim* s, rp_tune_report* report) {
+  SIM_OR_FAIL(s);
+  return s->e->autotune(report);
+}
+
+int rp_set_launch_shape(rp_sim* s, int bs_filter, int bs_force, int bs_accum, int grid_cap) {
+  SIM_OR_FAIL(s);
+  const int b[3] = {bs_filter, bs_force, bs_accum};
+  for (int k = 0; k < 3; ++k)
+    if (b[k] != 0 && (b[k] < 32 || b[k] > 256 || b[k] % 32 != 0)) {
+      set_error("block sizes must be multiples of 32 in [32, 256] (0 = default)");
+      return RP_E_INVALID_ARG;
+    }
+  if (grid_cap < 0) {
+    set_error("grid cap must be >= 0");
+    return RP_E_INVALID_ARG;
+  }
+  s->e->bs_filter = bs_filter;
+  s->e->bs_force = bs_force;
+  s->e->bs_accum = bs_accum;
+  s->e->grid_cap = grid_cap;
+  s->e->config_changed();
+  return RP_OK;
 }
 
 // ---------------------------------------------------------- learned JKR

@@ -49,6 +49,30 @@ struct Material {
   double E, nu, rho, mu, e, gamma;
 };
 
+// Constants of the pair and wall laws for one group of particles. A group is
+// an independent bed: its particles interact only with each other and with
+// the triangles of the group (or of GROUP_ALL), under the group's particle
+// material. Group 0 is the simulation's particle material; a simulation with
+// one group is exactly the reference's single-material simulation.
+struct Law {
+  double es_pp, es_pw, gs_pp;  // effective Young's moduli (pair, wall) and shear modulus (pair)
+  double gamma_pp, gamma_pw;   // combined surface energies
+  double beta_abs;             // |ln e / sqrt(ln^2 e + pi^2)| of the particle restitution (host libm)
+  double mu;                   // particle friction, used for pairs and walls (src/simulation.rs:489)
+  double jkr_C;                // 8 pi gamma / E* of pairs, as src/physics.rs:165 forms it
+  float jkr_Cf, pad_;
+};
+constexpr uint32_t GROUP_ALL = 0xFFFFFFFFu;
+
+// A rigid surface velocity V + W x (p - C) of a set of triangles whose geometry
+// stays put (a surface of revolution turning about its own axis, a belt). The
+// reference's walls are static; a wall with a motion enters the contact's
+// relative velocity at the contact point.
+struct WallMotion {
+  double c[3], w[3], v[3];
+};
+constexpr uint32_t NO_MOTION = 0xFFFFFFFFu;
+
 struct Bank {
   D4* xr;    // position, radius
   D4* vm;    // velocity, mass
@@ -65,13 +89,16 @@ struct Bank {
   uint32_t* nbr;    // neighbour rows, cap entries per slot
   uint32_t* ncnt;   // row lengths
   double* hist;     // physical-mode tangential spring per row entry: 3 planes of N*cap
+  uint32_t* grp;    // group (independent bed) of the slot
 };
 
 // Triangle record with the per-triangle constants of src/mesh.rs:45-62
 // precomputed (same operations, so the values are bit-identical).
 struct TriRec {
   double v0[3], e0[3], e1[3], n[3];
-  double a, b, c, det, denom, pad;
+  double a, b, c, det, denom;
+  uint32_t group;   // the group whose particles touch it (GROUP_ALL: every particle)
+  uint32_t motion;  // index into StepParams::motions, NO_MOTION for a static wall
   float4 plane;  // unit normal from the vertices and n.v0, FP32 (zero for a degenerate triangle)
   float4 bound;  // .x = largest |vertex coordinate| (scales the FP32 plane-test error)
   float4 edge[3];  // per edge: in-plane outward unit normal m and m.(edge start); (0,0,0,1e30) if degenerate
@@ -93,6 +120,10 @@ struct StepParams {
   int n;  // slots
   int cap;
   int force_path;  // 0: contact-parallel (default), 1: one thread per particle
+  // launch shapes of the force pass (chosen by the autotuner): threads per
+  // block of the filter, pair and accumulate kernels (<= 256), and the
+  // largest grid of their grid-stride loops
+  int bs_filter, bs_force, bs_accum, grid_cap;
   // contact-parallel buffers (recomputed every step)
   CRec* crec;       // n*cap records, row k at k*cap
   uint32_t* ccnt;   // records per particle
@@ -100,7 +131,8 @@ struct StepParams {
   uint32_t* coff;   // exclusive scan of ccnt: result offset of particle k
   uint32_t* poff;   // exclusive scan of ncomp
   uint32_t* clist;  // compact list of evaluating record slots
-  uint32_t* ctot;   // [0] records, [1] evaluating records, [2] network queue
+  uint32_t* ctot;   // [0] records, [1] evaluating records, [2] network queue, [3] deferred pairs
+  uint32_t* jfb;    // evaluating indices deferred to the reference-Newton pass (null: no deferral)
   double* cres;     // per record: force (3) and torque (3) on the row's particle
   uint32_t* cpart;  // scan partials
   int nmodel, tmodel, mode, prec;
@@ -110,9 +142,9 @@ struct StepParams {
   double bmin[3], bmax[3], bsize[3];
   double gravity[3];
   Material pm, wm;
-  double es_pp, es_pw, gs_pp;  // effective moduli (particle-particle, particle-wall)
-  double gamma_pp, gamma_pw;   // combined surface energies
-  double beta_abs;             // |ln e / sqrt(ln^2 e + pi^2)| of the particle restitution (host libm)
+  Law law;             // group 0 (the host's copy; kernels read glaw)
+  int ngroups;         // 1: no group array is read
+  const Law* glaw;     // per group, device array of ngroups entries
   // reference grid (parity-mode visit rule)
   double href, inv_href;
   int rdims[3];
@@ -132,11 +164,10 @@ struct StepParams {
   int tdims[3];
   const uint32_t* tstart;
   const uint32_t* titems;
+  const WallMotion* motions;
   // JKR solver for particle pairs: 0 the reference's Newton, 1 certificates +
   // network + polish, 2 certificates + FP32 Newton from the reference's start
   int jkr_solver;
-  double jkr_C;  // 8 pi gamma / E* of particle pairs, as the reference forms it
-  float jkr_Cf;
   float jdom_lo[4], jdom_hi[4];  // raw-feature range of the training set
   const MlpInfer* mlp;
   uint2* jq;        // network queue: (evaluating index, record slot); length ctot[2]
@@ -150,6 +181,12 @@ struct StepParams {
   Ctrl* ctrl;
   Bank bank[2];
 };
+
+// The law constants of slot k's group (a value copy: kernel parameters are
+// never addressed).
+__device__ __forceinline__ Law law_of(const StepParams& P, const Bank& B, int k) {
+  return P.glaw[P.ngroups > 1 ? B.grp[k] : 0u];
+}
 
 // ---- non-contracted double arithmetic (matches the oracle's rounding) ----
 __device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }

@@ -275,3 +275,23 @@ def test_neighbour_list_growth(rp, oracle_mod):
     o, g = one_step(rp, oracle_mod, st, 1, 0, lo, hi, dt=1e-7)
     assert g.stats()["status_bits"] & 4
     compare_step(o, g)
+
+
+def test_list_growth_inside_a_stepping_call(rp):
+    # the lists overflow at the first rebuild of a 10-step call of the device
+    # loop: the engine grows them, finishes the step and runs the remaining
+    # steps on a graph rebuilt for the new buffers; capacity never changes results
+    lo, hi = (-0.2, -0.2, -0.2), (0.2, 0.2, 0.2)
+    st = pu.random_bed(12, 4000, lo, hi, 0.004, 0.006, vscale=0.05, ascale=0.0, tscale=0.0)
+    runs = []
+    for cap in (4, 128):
+        g = pu.gpu_sim(rp, st, 1e-6, lo, hi, 4, 0, material=(1e7, 0.3, 2500.0, 0.5, 0.5, 0.05))
+        g.set_debug(False)
+        g.set_neighbor_capacity(cap)
+        g.steps(10)
+        runs.append((g.get_state(), g.stats()))
+    (s_small, st_small), (s_big, st_big) = runs
+    assert st_small["status_bits"] & 4 and not (st_big["status_bits"] & 4)
+    assert st_small["steps"] == st_big["steps"] == 10
+    np.testing.assert_array_equal(s_small["position"], s_big["position"])
+    np.testing.assert_array_equal(s_small["velocity"], s_big["velocity"])
