@@ -364,8 +364,8 @@ int Engine::alloc_lists(int cap, bool keep_current) {
 // evaluating record) and the device copy of the network, for the learned
 // JKR solver only.
 int Engine::ensure_jkr_buffers() {
-  // pairs left to the reference's Newton by the certified solvers, in FP64
-  const bool defer = gpu_ && jkr_solver != RP_JKR_NEWTON && nmodel == RP_NORMAL_JKR && prec == RP_PREC_FP64;
+  // pairs left to the reference's Newton by the certified solvers
+  const bool defer = gpu_ && jkr_solver != RP_JKR_NEWTON && nmodel == RP_NORMAL_JKR;
   if (defer) {
     const size_t need = std::max<size_t>(n_alloc_ * (size_t)std::max(cap_, 1), 1);
     if (jfb_alloc_ < need) {

@@ -829,6 +829,29 @@ __device__ __forceinline__ bool jkr_far_zero(const StepParams& P, float Cf, floa
   return x + kJkrKappa * c23 + 1e-3f < -(1e-5f * (fabsf(x) + c23 + 1e-3f) + 2.0f * e);
 }
 
+// Whether an sJKR pair certainly has zero normal force: overlap below
+// delta_c = -sqrt(3 pi^2 gamma^2 R* / E*^2) (src/physics.rs:234-325; with
+// gamma <= 0 the law is Hertz's, zero for a negative overlap), decided on the
+// FP32 mirror with its rounding (as jkr_far_zero) and 1e-5 of delta_c as
+// margin. Symmetric in (i, j) bit for bit.
+__device__ __forceinline__ bool sjkr_far_zero(const StepParams& P, const Law& L, float4 xif, float Xi, float4 xjf) {
+  float fx = xif.x - xjf.x, fy = xif.y - xjf.y, fz = xif.z - xjf.z;
+  if (P.periodic[0]) { const float Lp = (float)P.bsize[0]; if (fx > 0.5f * Lp) fx -= Lp; else if (fx < -0.5f * Lp) fx += Lp; }
+  if (P.periodic[1]) { const float Lp = (float)P.bsize[1]; if (fy > 0.5f * Lp) fy -= Lp; else if (fy < -0.5f * Lp) fy += Lp; }
+  if (P.periodic[2]) { const float Lp = (float)P.bsize[2]; if (fz > 0.5f * Lp) fz -= Lp; else if (fz < -0.5f * Lp) fz += Lp; }
+  const float rsum = xif.w + xjf.w;
+  const float rs = (xif.w * xjf.w) / rsum;
+  const float d = sqrtf(fx * fx + fy * fy + fz * fz);
+  const float X = fmaxf(Xi, fmaxf(fmaxf(fabsf(xjf.x), fabsf(xjf.y)), fabsf(xjf.z)));
+  const float e = 1.8e-7f * (2.0f * X + 3.0f * rsum + P.lmax) + 4e-7f * (d + rsum);
+  float dc = 0.0f;
+  if (L.gamma_pp > 0.0) {
+    const float g = (float)L.gamma_pp, es = (float)L.es_pp, pi = 3.14159265f;
+    dc = -sqrtf(3.0f * (pi * pi) * (g * g) * rs / (es * es));
+  }
+  return (rsum - d) + e < dc - 1e-5f * fabsf(dc);
+}
+
 // Pass 1 (FP32 and integer work only): the candidates of each particle, i.e.
 // list entries the FP32 pretest cannot rule out and that the reference's loop
 // visits from this end (visit counts from both ends recorded); counts all
@@ -848,6 +871,8 @@ __global__ void __launch_bounds__(256) k_contact_filter(StepParams P) {
   // candidates at all. Parity-mode springs (G* = 0, NaN for Mindlin at
   // negative overlap) and debug recording keep every pair.
   const bool zdrop_any = P.jkr_solver != 0 && P.nmodel == 3 && P.pretest && !P.debug && (P.tmodel == 0 || PHYS);
+  // the same for sJKR, whose zero region is explicit (no iteration to certify)
+  const bool sdrop = P.nmodel == 4 && P.pretest && !P.debug && (P.tmodel == 0 || PHYS);
   const size_t plane = (size_t)P.n * P.cap;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < P.n; k += gridDim.x * blockDim.x) {
     uint32_t nrec = 0, ncmp = 0, nnet = 0;
@@ -866,7 +891,8 @@ __global__ void __launch_bounds__(256) k_contact_filter(StepParams P) {
         const size_t hi = (size_t)k * P.cap + m;
         int vij = 0, vji = 0;
         const float4 xjf = B.xf[j];
-        if (!(P.pretest && pretest_far(P, xif, Xi, xjf, adh)) && !(zdrop && jkr_far_zero(P, lw.jkr_Cf, xif, Xi, xjf))) {
+        if (!(P.pretest && pretest_far(P, xif, Xi, xjf, adh)) && !(zdrop && jkr_far_zero(P, lw.jkr_Cf, xif, Xi, xjf)) &&
+            !(sdrop && sjkr_far_zero(P, lw, xif, Xi, xjf))) {
           if (PHYS) {
             vij = vji = 1;
           } else {
@@ -985,9 +1011,9 @@ __global__ void __launch_bounds__(128) k_jkr_mlp(StepParams P) {
 // with its own torque (n r_j) x (-f), and in physical mode the negated spring.
 // A candidate outside the cutoff gives zero results at both ends.
 //
-// With a certified JKR solver in FP64, a pair whose JKR force needs the
-// reference's own Newton iteration (up to 20 FP64 steps) is not evaluated in
-// this pass: it would hold its whole warp for those steps. It is appended to
+// With a certified JKR solver, a pair whose JKR force needs the reference's
+// own Newton iteration (up to 20 steps) is not evaluated in this pass: it
+// would hold its whole warp for those steps. It is appended to
 // a deferred list (contact_eval returns true) and k_contact_deferred
 // evaluates the deferred pairs densely; each pair writes the same result slots
 // in either pass, so the outcome does not depend on the order.
@@ -1016,7 +1042,7 @@ __device__ __forceinline__ bool contact_eval(const StepParams& P, const Bank& B,
     const D4 vi4 = B.vm[k], wi4 = B.wc[k], vj4 = B.vm[j], wj4 = B.wc[j];
     const Law lw = law_of(P, B, (int)k);
     bool deferred = false;
-    const bool can_defer = first_pass && sizeof(R) == sizeof(double) && P.jfb != nullptr;
+    const bool can_defer = first_pass && P.jfb != nullptr;
     if (!pair_contact<R, PHYS, HIST>(P, lw, d, d2, rsum, xi4.w, xj4.w, vi4.w, vj4.w, xyz(vi4), xyz(vj4), xyz(wi4),
                                      xyz(wj4), hk, plane, fc, tc, nrm, excess, guess, tally,
                                      can_defer ? &deferred : nullptr, !first_pass))
@@ -1249,7 +1275,7 @@ static int launch_contact_path(const StepParams& P, cudaStream_t s) {
   if (P.mode == 0) k_contact_force<false, false, R><<<gc, bc, 0, s>>>(P);
   else if (hist) k_contact_force<true, true, R><<<gc, bc, 0, s>>>(P);
   else k_contact_force<true, false, R><<<gc, bc, 0, s>>>(P);
-  if (P.jfb != nullptr && sizeof(R) == sizeof(double)) {
+  if (P.jfb != nullptr) {
     if (P.mode == 0) k_contact_deferred<false, false, R><<<152 * 8, 128, 0, s>>>(P);
     else if (hist) k_contact_deferred<true, true, R><<<152 * 8, 128, 0, s>>>(P);
     else k_contact_deferred<true, false, R><<<152 * 8, 128, 0, s>>>(P);

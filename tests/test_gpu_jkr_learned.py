@@ -195,6 +195,35 @@ def test_learned_forces_match_fp64_oracle(rp, oracle_mod, trained, solver):
         assert 2 * cnt["accepted"] <= cnt["fp32_newton_steps"] <= 2 * (cnt["accepted"] + cnt["fallback"]), cnt
 
 
+@pytest.mark.parametrize("normal,solver", [(3, "certified"), (3, "learned"), (4, "newton")])
+def test_dropped_zero_pairs_match_oracle(rp, oracle_mod, trained, normal, solver):
+    # without debug recording, pairs certified to add exactly +-0 (JKR beyond
+    # pull-off; sJKR below delta_c) are dropped in the filter: the step must
+    # still match the oracle (velocities carry the forces of the step)
+    params, norm, dom = trained[0]
+    st, lo, hi = _jkr_bed(73, 3000, 3.0e-4)
+    per = (True, True, True)
+    o = pu.oracle_sim(oracle_mod, st, 1e-9, lo, hi, normal, 0, periodic=per, material=MAT)
+    g = pu.gpu_sim(rp, st, 1e-9, lo, hi, normal, 0, periodic=per, material=MAT)
+    g.set_debug(False)
+    g.set_jkr_network(params, norm, dom)
+    g.set_jkr_solver(solver)
+    o.steps(2)
+    g.steps(2)
+    so, sg = o.state(), g.get_state()
+    FS, TS = o.last_force_scale()
+    np.testing.assert_array_equal(np.isfinite(sg["velocity"]), np.isfinite(so["v"]))
+    # forces within 1e-6 of each particle's sum of contact-force magnitudes,
+    # over two steps of dt
+    dt = 1e-9
+    inertia = 0.4 * st["mass"] * st["radius"] ** 2
+    tv = 4e-6 * FS / st["mass"] * dt + 1e-15
+    tw = 4e-6 * TS / inertia * dt + 1e-12
+    assert np.all(np.abs(sg["velocity"] - so["v"]).max(1) <= tv)
+    assert np.all(np.abs(sg["angular_velocity"] - so["w"]).max(1) <= tw)
+    assert np.all(np.abs(sg["position"] - so["x"]).max(1) <= tv * dt + 1e-18)
+
+
 def test_learned_mixed_precision_within_1e5(rp, oracle_mod, trained):
     ef, et, cnt = _forces_vs_oracle(rp, oracle_mod, trained[0], "learned", precision=1)
     assert ef <= 1e-5 and et <= 1e-5, (ef, et, cnt)
