@@ -718,7 +718,7 @@ int Engine::upload() {
     a8[3][i] = D4{p.a[0], p.a[1], p.a[2], 0.0};
     a8[4][i] = D4{p.tau[0], p.tau[1], p.tau[2], 0.0};
     a8[5][i] = D4{p.xres[0], p.xres[1], p.xres[2], 0.0};
-    a8[6][i] = D4{p.vres[0], p.vres[1], p.vres[2], 0.0};
+    a8[6][i] = D4{p.vres[0], p.vres[1], p.vres[2], 1.0 / p.m};  // .w carries 1/m
     // .w carries 1 / I = 1 / (0.4 m r^2) (constant per particle; the same
     // correctly rounded division the step would do)
     a8[7][i] = D4{p.wres[0], p.wres[1], p.wres[2], 1.0 / (0.4 * p.m * p.r * p.r)};

@@ -400,6 +400,15 @@ __device__ __forceinline__ bool pair_contact(const StepParams& P, const Law& L, 
   return true;
 }
 
+// Kahan-compensated s += d with residual r (src/particle.rs:12-18 and the
+// reference's integrator): y = d - r, t = s + y, r = (t - s) - y, s = t.
+__device__ __forceinline__ void kahan_add(V& s, V& r, V d) {
+  const V y = d - r;
+  const V t = s + y;
+  r = (t - s) - y;
+  s = t;
+}
+
 // Second half of velocity Verlet for one particle (src/simulation.rs:541-561):
 // Kahan-compensated v += a dt/2 and omega += (tau/I) dt/2, I = 0.4 m r^2
 // (tau/I as tau * (1/I), 1/I stored per particle in Bank::wres[k].w when the
@@ -444,17 +453,26 @@ __global__ void __launch_bounds__(256) k_first_half(StepParams P) {
     D4 xr = B.xr[k], vm = B.vm[k], wc = B.wc[k];
     V x = xyz(xr), v = xyz(vm), w = xyz(wc);
     const bool moving = !(fl & PF_FIXED);
-    V a = vmk(0.0, 0.0, 0.0), tau = a, vres = a, wres = a, xres = a;
-    double inv_inertia = 0.0;
+    V vres = vmk(0.0, 0.0, 0.0), wres = vres, xres = vres, dv = vres, dw = vres;
+    double inv_inertia = 0.0, inv_mass = 0.0;
     if (moving) {
-      a = xyz(B.acc[k]);
-      tau = xyz(B.tq[k]);
-      vres = xyz(B.vres[k]);
+      // the fused second half of the previous step and this step's first
+      // half kick with the same a and tau: the increments are computed once
+      const V a = xyz(B.acc[k]);
+      const V tau = xyz(B.tq[k]);
+      const D4 vr4 = B.vres[k];
+      vres = xyz(vr4);
+      inv_mass = vr4.w;
       const D4 wr4 = B.wres[k];
       wres = xyz(wr4);
       inv_inertia = wr4.w;
       xres = xyz(B.xres[k]);
-      if (FUSE) second_half_kick(v, vres, w, wres, a, tau, inv_inertia, dt);
+      dv = (0.5 * a) * dt;
+      dw = (0.5 * (tau * inv_inertia)) * dt;
+      if (FUSE) {
+        kahan_add(v, vres, dv);
+        kahan_add(w, wres, dw);
+      }
     }
     if (anyp) {
       if (P.periodic[0]) { if (x.x < P.bmin[0]) x.x = x.x + P.bsize[0]; else if (x.x >= P.bmax[0]) x.x = x.x - P.bsize[0]; }
@@ -475,24 +493,11 @@ __global__ void __launch_bounds__(256) k_first_half(StepParams P) {
       continue;
     }
     if (moving) {
-      V dv = (0.5 * a) * dt;
-      V yv = dv - vres;
-      V tv = v + yv;
-      vres = (tv - v) - yv;
-      v = tv;
-      V dx = v * dt;
-      V yx = dx - xres;
-      V tx = x + yx;
-      xres = (tx - x) - yx;
-      x = tx;
-      V aa = tau * inv_inertia;
-      V dw = (0.5 * aa) * dt;
-      V yw = dw - wres;
-      V tw = w + yw;
-      wres = (tw - w) - yw;
-      w = tw;
+      kahan_add(v, vres, dv);
+      kahan_add(x, xres, v * dt);
+      kahan_add(w, wres, dw);
       B.vm[k] = D4{v.x, v.y, v.z, vm.w};
-      B.vres[k] = D4{vres.x, vres.y, vres.z, 0.0};
+      B.vres[k] = D4{vres.x, vres.y, vres.z, inv_mass};
       B.xres[k] = D4{xres.x, xres.y, xres.z, 0.0};
       B.wres[k] = D4{wres.x, wres.y, wres.z, inv_inertia};
       wc.x = w.x; wc.y = w.y; wc.z = w.z;
@@ -526,12 +531,12 @@ __global__ void __launch_bounds__(256) k_second_half(StepParams P) {
     uint32_t fl = B.flags[k];
     if (fl & (PF_DEAD | PF_FIXED)) continue;
     D4 vm = B.vm[k], wc = B.wc[k];
-    const D4 wr4 = B.wres[k];
-    V v = xyz(vm), w = xyz(wc), vres = xyz(B.vres[k]), wres = xyz(wr4);
+    const D4 wr4 = B.wres[k], vr4 = B.vres[k];
+    V v = xyz(vm), w = xyz(wc), vres = xyz(vr4), wres = xyz(wr4);
     second_half_kick(v, vres, w, wres, xyz(B.acc[k]), xyz(B.tq[k]), wr4.w, P.dt);
     B.vm[k] = D4{v.x, v.y, v.z, vm.w};
     B.wc[k] = D4{w.x, w.y, w.z, wc.w};
-    B.vres[k] = D4{vres.x, vres.y, vres.z, 0.0};
+    B.vres[k] = D4{vres.x, vres.y, vres.z, vr4.w};
     B.wres[k] = D4{wres.x, wres.y, wres.z, wr4.w};
   }
 }
@@ -735,9 +740,10 @@ __global__ void __launch_bounds__(128) k_force(StepParams P) {
       P.dbgT[3 * (size_t)k] = T.x; P.dbgT[3 * (size_t)k + 1] = T.y; P.dbgT[3 * (size_t)k + 2] = T.z;
     }
     if (!isfinite(F.x + F.y + F.z + T.x + T.y + T.z)) atomicOr(&C->status, (unsigned)ST_NAN);
-    // apply (src/simulation.rs:532-536); the second half kick of this step
-    // runs in the next k_first_half or in k_second_half
-    const V a = vmk(P.gravity[0], P.gravity[1], P.gravity[2]) + F / mi;
+    // apply (src/simulation.rs:532-536), F/m as F (1/m) with 1/m stored per
+    // particle; the second half kick of this step runs in the next
+    // k_first_half or in k_second_half
+    const V a = vmk(P.gravity[0], P.gravity[1], P.gravity[2]) + F * B.vres[k].w;
     const V tau = vmk(0.0, 0.0, 0.0) + T;
     B.acc[k] = D4{a.x, a.y, a.z, 0.0};
     B.tq[k] = D4{tau.x, tau.y, tau.z, 0.0};
@@ -1057,9 +1063,14 @@ __device__ __forceinline__ bool contact_eval(const StepParams& P, const Bank& B,
   }
   if (P.debug) P.dbgMult[hik] = (uint8_t)(in ? vij : 0);
   double* out = P.cres + 6 * (size_t)(P.coff[k] + c);
-  const double sv = (double)vij;
-  out[0] = fc.x * sv; out[1] = fc.y * sv; out[2] = fc.z * sv;
-  out[3] = tc.x * sv; out[4] = tc.y * sv; out[5] = tc.z * sv;
+  if (vij == 1) {  // x * 1 = x: no FP64 multiply for the common single visit
+    out[0] = fc.x; out[1] = fc.y; out[2] = fc.z;
+    out[3] = tc.x; out[4] = tc.y; out[5] = tc.z;
+  } else {
+    const double sv = (double)vij;
+    out[0] = fc.x * sv; out[1] = fc.y * sv; out[2] = fc.z * sv;
+    out[3] = tc.x * sv; out[4] = tc.y * sv; out[5] = tc.z * sv;
+  }
   if (vji > 0) {
     const uint32_t nj = P.ccnt[j];
     const CRec* rj = P.crec + (size_t)j * P.cap;
@@ -1074,9 +1085,14 @@ __device__ __forceinline__ bool contact_eval(const StepParams& P, const Bank& B,
         t2 = cross(nrm * xj4.w, f2);
       }
       double* o2 = P.cres + 6 * (size_t)(P.coff[j] + c2);
-      const double s2 = (double)vji;
-      o2[0] = f2.x * s2; o2[1] = f2.y * s2; o2[2] = f2.z * s2;
-      o2[3] = t2.x * s2; o2[4] = t2.y * s2; o2[5] = t2.z * s2;
+      if (vji == 1) {
+        o2[0] = f2.x; o2[1] = f2.y; o2[2] = f2.z;
+        o2[3] = t2.x; o2[4] = t2.y; o2[5] = t2.z;
+      } else {
+        const double s2 = (double)vji;
+        o2[0] = f2.x * s2; o2[1] = f2.y * s2; o2[2] = f2.z * s2;
+        o2[3] = t2.x * s2; o2[4] = t2.y * s2; o2[5] = t2.z * s2;
+      }
       const size_t h2 = (size_t)j * P.cap + (rj[c2].mv & 0xFFFFu);
       if (HIST) {
         B.hist[h2] = -hk[0];
@@ -1163,7 +1179,7 @@ __global__ void __launch_bounds__(256) k_accumulate(StepParams P) {
       P.dbgT[3 * (size_t)k] = T.x; P.dbgT[3 * (size_t)k + 1] = T.y; P.dbgT[3 * (size_t)k + 2] = T.z;
     }
     if (!isfinite(F.x + F.y + F.z + T.x + T.y + T.z)) atomicOr(&C->status, (unsigned)ST_NAN);
-    const V a = vmk(P.gravity[0], P.gravity[1], P.gravity[2]) + F / mi;
+    const V a = vmk(P.gravity[0], P.gravity[1], P.gravity[2]) + F * B.vres[k].w;  // F (1/m)
     const V tau = vmk(0.0, 0.0, 0.0) + T;
     B.acc[k] = D4{a.x, a.y, a.z, 0.0};
     B.tq[k] = D4{tau.x, tau.y, tau.z, 0.0};
