@@ -45,6 +45,11 @@ using V = T3<double>;
 using Vf = T3<float>;
 __device__ __forceinline__ V vmk(double x, double y, double z) { return V{x, y, z}; }
 __device__ __forceinline__ V xyz(const D4& d) { return V{d.x, d.y, d.z}; }
+// isfinite(x) and 0.0 + x from the bits, off the FP64 pipe
+__device__ __forceinline__ bool finite_bits(double x) { return (__double2hiint(x) & 0x7ff00000) != 0x7ff00000; }
+__device__ __forceinline__ double plus_zero(double x) {
+  return (__double_as_longlong(x) << 1) == 0 ? 0.0 : x;
+}
 
 constexpr double kPi = 3.14159265358979323846;
 
@@ -415,13 +420,14 @@ __device__ __forceinline__ void kahan_add(V& s, V& r, V d) {
 // state is uploaded; v and x are unchanged).
 __device__ __forceinline__ void second_half_kick(V& v, V& vres, V& w, V& wres, V a, V tau, double inv_inertia,
                                                  double dt) {
-  V dv = (0.5 * a) * dt;
+  const double hdt = 0.5 * dt;  // (0.5 a) dt == a (0.5 dt), both one rounding of a dt / 2
+  V dv = a * hdt;
   V yv = dv - vres;
   V tv = v + yv;
   vres = (tv - v) - yv;
   v = tv;
   V aa = tau * inv_inertia;
-  V dw = (0.5 * aa) * dt;
+  V dw = aa * hdt;
   V yw = dw - wres;
   V tw = w + yw;
   wres = (tw - w) - yw;
@@ -446,6 +452,10 @@ __global__ void __launch_bounds__(256) k_first_half(StepParams P) {
   const double dt = P.dt;
   const bool anyp = P.periodic[0] | P.periodic[1] | P.periodic[2];
   const float half_skin = (float)(0.5 * P.skin);
+  // (0.5 a) dt and a (0.5 dt) are the same correctly rounded product
+  const double hdt = 0.5 * dt;
+  const float bminf[3] = {(float)P.bmin[0], (float)P.bmin[1], (float)P.bmin[2]};
+  const float inv_hf = (float)P.inv_href;
   bool want_rebuild = false;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < P.n; k += gridDim.x * blockDim.x) {
     uint32_t fl = B.flags[k];
@@ -467,8 +477,8 @@ __global__ void __launch_bounds__(256) k_first_half(StepParams P) {
       wres = xyz(wr4);
       inv_inertia = wr4.w;
       xres = xyz(B.xres[k]);
-      dv = (0.5 * a) * dt;
-      dw = (0.5 * (tau * inv_inertia)) * dt;
+      dv = a * hdt;
+      dw = (tau * inv_inertia) * hdt;
       if (FUSE) {
         kahan_add(v, vres, dv);
         kahan_add(w, wres, dw);
@@ -502,16 +512,18 @@ __global__ void __launch_bounds__(256) k_first_half(StepParams P) {
       B.wres[k] = D4{wres.x, wres.y, wres.z, inv_inertia};
       wc.x = w.x; wc.y = w.y; wc.z = w.z;
     }
+    const float4 xf = make_float4((float)x.x, (float)x.y, (float)x.z, (float)xr.w);
     if (P.mode == 0) {
-      int32_t c[3];
-      ref_coords(P, x.x, x.y, x.z, c);
-      wc.w = __longlong_as_double((long long)pack_code(c[0], c[1], c[2]));
+      const int32_t c0 = ref_axis_fast(x.x, xf.x, P.bmin[0], bminf[0], P.href, P.inv_href, inv_hf);
+      const int32_t c1 = ref_axis_fast(x.y, xf.y, P.bmin[1], bminf[1], P.href, P.inv_href, inv_hf);
+      const int32_t c2 = ref_axis_fast(x.z, xf.z, P.bmin[2], bminf[2], P.href, P.inv_href, inv_hf);
+      wc.w = __longlong_as_double((long long)pack_code(c0, c1, c2));
     }
     B.wc[k] = wc;
     B.xr[k] = D4{x.x, x.y, x.z, xr.w};
-    B.xf[k] = make_float4((float)x.x, (float)x.y, (float)x.z, (float)xr.w);
+    B.xf[k] = xf;
     float4 r0 = B.xref[k];
-    float ddx = (float)x.x - r0.x, ddy = (float)x.y - r0.y, ddz = (float)x.z - r0.z;
+    float ddx = xf.x - r0.x, ddy = xf.y - r0.y, ddz = xf.z - r0.z;
     if (P.periodic[0]) ddx -= (float)P.bsize[0] * rintf(ddx / (float)P.bsize[0]);
     if (P.periodic[1]) ddy -= (float)P.bsize[1] * rintf(ddy / (float)P.bsize[1]);
     if (P.periodic[2]) ddz -= (float)P.bsize[2] * rintf(ddz / (float)P.bsize[2]);
@@ -1155,13 +1167,65 @@ __global__ void __launch_bounds__(128) k_contact_deferred(StepParams P) {
 
 // Pass 4: per particle, the contact results in list order, the walls, then
 // a = g + F/m and tau = T (src/simulation.rs:265-271, 532-536).
+// Threads take their block's particles in the order of a shared-memory
+// counting sort by (triangles listed in the particle's cell, contact count),
+// so a warp's lanes run loops of similar length; each particle's arithmetic
+// is the same whatever thread runs it.
+constexpr uint32_t ACC_BINS = 128;
+
+__device__ __forceinline__ bool tri_cell_nonempty(const StepParams& P, float4 xf) {
+  const float q0 = floorf((xf.x - P.tminf[0]) * P.tinvf);
+  const float q1 = floorf((xf.y - P.tminf[1]) * P.tinvf);
+  const float q2 = floorf((xf.z - P.tminf[2]) * P.tinvf);
+  if (!(q0 >= 0.f && q1 >= 0.f && q2 >= 0.f && q0 < (float)P.tdims[0] && q1 < (float)P.tdims[1] &&
+        q2 < (float)P.tdims[2]))
+    return false;
+  const uint32_t cell = (uint32_t)q0 + (uint32_t)P.tdims[0] * ((uint32_t)q1 + (uint32_t)P.tdims[1] * (uint32_t)q2);
+  return P.tstart[cell + 1] > P.tstart[cell];
+}
+
 __global__ void __launch_bounds__(256) k_accumulate(StepParams P) {
   Ctrl* C = P.ctrl;
   if (C->halt) return;
   const Bank B = P.bank[C->bank];
+  __shared__ uint32_t bins[ACC_BINS];
+  __shared__ uint16_t order[256];
   bool excess = false;
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < P.n; k += gridDim.x * blockDim.x) {
-    if (B.flags[k] & PF_DEAD) continue;
+  for (int base = blockIdx.x * blockDim.x; base < P.n; base += gridDim.x * blockDim.x) {
+    {
+      const int k0 = base + threadIdx.x;
+      uint32_t key = ACC_BINS - 1;
+      if (k0 < P.n && !(B.flags[k0] & PF_DEAD)) {
+        key = min(P.ccnt[k0], 63u);
+        if (P.ntri > 0 && tri_cell_nonempty(P, B.xf[k0])) key += 64;
+      }
+      for (uint32_t i = threadIdx.x; i < ACC_BINS; i += blockDim.x) bins[i] = 0;
+      __syncthreads();
+      const uint32_t rank = atomicAdd(&bins[key], 1u);
+      __syncthreads();
+      if (threadIdx.x < 32) {  // exclusive scan of the bins, four per lane
+        const uint32_t l = threadIdx.x;
+        const uint32_t c0 = bins[4 * l], c1 = bins[4 * l + 1], c2 = bins[4 * l + 2], c3 = bins[4 * l + 3];
+        const uint32_t sum = c0 + c1 + c2 + c3;
+        uint32_t incl = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+          if (l >= (uint32_t)o) incl += t;
+        }
+        const uint32_t ex = incl - sum;
+        bins[4 * l] = ex;
+        bins[4 * l + 1] = ex + c0;
+        bins[4 * l + 2] = ex + c0 + c1;
+        bins[4 * l + 3] = ex + c0 + c1 + c2;
+      }
+      __syncthreads();
+      order[bins[key] + rank] = (uint16_t)threadIdx.x;
+      __syncthreads();
+    }
+    const int k = base + order[threadIdx.x];
+    __syncthreads();  // order and bins are rewritten for the next tile
+    if (k >= P.n || (B.flags[k] & PF_DEAD)) continue;
     V F = vmk(0.0, 0.0, 0.0), T = vmk(0.0, 0.0, 0.0);
     const uint32_t n = P.ccnt[k];
     const double* res = P.cres + 6 * (size_t)P.coff[k];
@@ -1169,18 +1233,21 @@ __global__ void __launch_bounds__(256) k_accumulate(StepParams P) {
       F = F + vmk(res[6 * c], res[6 * c + 1], res[6 * c + 2]);
       T = T + vmk(res[6 * c + 3], res[6 * c + 4], res[6 * c + 5]);
     }
-    const D4 xi4 = B.xr[k], vi4 = B.vm[k], wi4 = B.wc[k];
-    const double mi = vi4.w;
-    if (P.ntri > 0)
+    if (P.ntri > 0) {
+      const D4 xi4 = B.xr[k], vi4 = B.vm[k], wi4 = B.wc[k];
       wall_forces(P, law_of(P, B, k), P.ngroups > 1 ? B.grp[k] : 0u, xyz(xi4), B.xf[k], xyz(vi4), xyz(wi4), xi4.w,
-                  mi, F, T, excess);
+                  vi4.w, F, T, excess);
+    }
     if (P.debug) {
       P.dbgF[3 * (size_t)k] = F.x; P.dbgF[3 * (size_t)k + 1] = F.y; P.dbgF[3 * (size_t)k + 2] = F.z;
       P.dbgT[3 * (size_t)k] = T.x; P.dbgT[3 * (size_t)k + 1] = T.y; P.dbgT[3 * (size_t)k + 2] = T.z;
     }
-    if (!isfinite(F.x + F.y + F.z + T.x + T.y + T.z)) atomicOr(&C->status, (unsigned)ST_NAN);
+    // non-finite check and the +0 of 0 + T on the integer pipe
+    if (!(finite_bits(F.x) & finite_bits(F.y) & finite_bits(F.z) & finite_bits(T.x) & finite_bits(T.y) &
+          finite_bits(T.z)))
+      atomicOr(&C->status, (unsigned)ST_NAN);
     const V a = vmk(P.gravity[0], P.gravity[1], P.gravity[2]) + F * B.vres[k].w;  // F (1/m)
-    const V tau = vmk(0.0, 0.0, 0.0) + T;
+    const V tau = vmk(plus_zero(T.x), plus_zero(T.y), plus_zero(T.z));
     B.acc[k] = D4{a.x, a.y, a.z, 0.0};
     B.tq[k] = D4{tau.x, tau.y, tau.z, 0.0};
   }

@@ -229,6 +229,21 @@ __device__ __forceinline__ double floor_div_exact(double d, double h, double inv
   return f;
 }
 
+// One axis of the reference cell from the FP32 mirror xf of x when that is
+// provably the FP64 answer. With A = (|xf| + |bf|)/h, the FP32 quotient
+// (xf - bf)(1/h) lies within 2^-24 A + 3 2^-24 |q| of the FP64 one (rounding
+// of x, b, 1/h, the difference and the product); when no integer lies within
+// 2^-21 (A + |q| + 1) of it, both floors agree. Otherwise (and for NaN, inf or
+// |q| >= 2^22) the exact FP64 path decides.
+__device__ __forceinline__ int32_t ref_axis_fast(double x, float xf, double b, float bf, double h, double inv_h,
+                                                 float inv_hf) {
+  const float q = (xf - bf) * inv_hf;
+  const float f = floorf(q);
+  const float tol = 4.76837158203125e-7f * ((fabsf(xf) + fabsf(bf)) * inv_hf + fabsf(q) + 1.0f);
+  if (q - f > tol && (f + 1.0f) - q > tol) return (int32_t)f;
+  return sat_i32(floor_div_exact(dsub(x, b), h, inv_h));
+}
+
 // Reference cell coordinates of a position (src/grid.rs:30-32).
 __device__ __forceinline__ void ref_coords(const StepParams& P, double x, double y, double z, int32_t c[3]) {
   c[0] = sat_i32(floor_div_exact(dsub(x, P.bmin[0]), P.href, P.inv_href));

@@ -99,6 +99,31 @@ def test_one_step_periodic(rp, oracle_mod, periodic):
     compare_step(o, g)
 
 
+@pytest.mark.parametrize("h", [0.1, 0.03])
+def test_one_step_particles_on_cell_faces(rp, oracle_mod, h):
+    # a touching lattice with pitch h whose sites sit on reference-cell faces,
+    # each coordinate moved by -3..3 ulps: the cell of a site is decided by the
+    # rounding of (x - min) / h, and a neighbour one cell further off is not
+    # visited at all (src/grid.rs:54-85), so the pair multiset shows any cell
+    # taken from an inexact quotient
+    lo, hi = (-0.45, -0.45, -0.45), (0.45, 0.45, 0.45)
+    rng = np.random.default_rng(int(h * 1000))
+    m = min(int(0.9 / h) - 1, 14)
+    g3 = np.stack(np.meshgrid(*[np.arange(1, m + 1)] * 3, indexing="ij"), -1).reshape(-1, 3)
+    x = np.asarray(lo) + g3 * h
+    steps = rng.integers(-3, 4, x.shape)
+    for it in range(3):
+        sel = np.abs(steps) > it
+        x[sel] = np.nextafter(x[sel], np.sign(steps[sel]) * np.inf)
+    k = len(x)
+    r = np.full(k, 0.51 * h)
+    st = {"position": x, "radius": r, "mass": 2500.0 * 4.0 / 3.0 * np.pi * r ** 3, "velocity": np.zeros((k, 3)),
+          "angular_velocity": np.zeros((k, 3)), "acceleration": np.zeros((k, 3)), "torque": np.zeros((k, 3)),
+          "fixed": np.zeros(k, np.uint8)}
+    o, g = one_step(rp, oracle_mod, st, 1, 0, lo, hi, cell=h)
+    compare_step(o, g)
+
+
 def test_one_step_small_periodic_box_double_visits(rp, oracle_mod):
     # cell size equal to the periodic size: dims = ceil(L/h)+1 = 2, so a
     # particle that drifted past the +x face during the step sits in cell 1,
