@@ -67,6 +67,46 @@ Law Engine::make_law(const Material& m) const {
   return L;
 }
 
+// Squared distance from p to the triangle (a, b, c): the closest point by
+// its Voronoi region (Ericson, Real-Time Collision Detection, 2005, 5.1.5).
+static double point_triangle_dist2(const double p[3], const double a[3], const double b[3], const double c[3]) {
+  auto sub = [](const double* u, const double* v, double* w) { for (int k = 0; k < 3; ++k) w[k] = u[k] - v[k]; };
+  auto dot = [](const double* u, const double* v) { return u[0] * v[0] + u[1] * v[1] + u[2] * v[2]; };
+  auto d2to = [&](const double* q) { double w[3]; sub(p, q, w); return dot(w, w); };
+  double ab[3], ac[3], ap[3], bp[3], cp[3], q[3];
+  sub(b, a, ab); sub(c, a, ac); sub(p, a, ap);
+  const double d1 = dot(ab, ap), d2 = dot(ac, ap);
+  if (d1 <= 0.0 && d2 <= 0.0) return dot(ap, ap);
+  sub(p, b, bp);
+  const double d3 = dot(ab, bp), d4 = dot(ac, bp);
+  if (d3 >= 0.0 && d4 <= d3) return dot(bp, bp);
+  const double vc = d1 * d4 - d3 * d2;
+  if (vc <= 0.0 && d1 >= 0.0 && d3 <= 0.0) {
+    const double v = d1 / (d1 - d3);
+    for (int k = 0; k < 3; ++k) q[k] = a[k] + v * ab[k];
+    return d2to(q);
+  }
+  sub(p, c, cp);
+  const double d5 = dot(ab, cp), d6 = dot(ac, cp);
+  if (d6 >= 0.0 && d5 <= d6) return dot(cp, cp);
+  const double vb = d5 * d2 - d1 * d6;
+  if (vb <= 0.0 && d2 >= 0.0 && d6 <= 0.0) {
+    const double w = d2 / (d2 - d6);
+    for (int k = 0; k < 3; ++k) q[k] = a[k] + w * ac[k];
+    return d2to(q);
+  }
+  const double va = d3 * d6 - d5 * d4;
+  if (va <= 0.0 && d4 - d3 >= 0.0 && d5 - d6 >= 0.0) {
+    const double w = (d4 - d3) / ((d4 - d3) + (d5 - d6));
+    for (int k = 0; k < 3; ++k) q[k] = b[k] + w * (c[k] - b[k]);
+    return d2to(q);
+  }
+  const double den = 1.0 / (va + vb + vc);
+  const double v = vb * den, w = vc * den;
+  for (int k = 0; k < 3; ++k) q[k] = a[k] + ab[k] * v + ac[k] * w;
+  return d2to(q);
+}
+
 static int bits_for(uint64_t maxkey) {
   int b = 1;
   while (b < 32 && (1ull << b) <= maxkey) ++b;
@@ -120,7 +160,7 @@ void Engine::free_device() {
   dfree(rb_.ka); dfree(rb_.va); dfree(rb_.kb); dfree(rb_.vb); dfree(rb_.hist); dfree(rb_.part);
   dfree(rb_.cstart); dfree(rb_.cend); dfree(kraw_);
   dfree(dbgF_); dfree(dbgT_); dfree(dbgMult_); dfree(ke_);
-  dfree(crec_); dfree(clist_); dfree(cres_); dfree(ccnt_); dfree(ncomp_); dfree(coff_); dfree(poff_);
+  dfree(crec_); dfree(clist_); dfree(cres_); dfree(ccnt_); dfree(aorder_); dfree(wq_); dfree(wcand_); dfree(ncomp_); dfree(coff_); dfree(poff_);
   dfree(ctot_); dfree(cpart_);
   dfree(tri_d_); dfree(tstart_d_); dfree(titems_d_); dfree(glaw_d_); dfree(motions_d_);
   dfree(mlp_d_); dfree(jq_); dfree(jguess_); dfree(nnet_); dfree(noff_); dfree(jfb_);
@@ -299,10 +339,11 @@ int Engine::alloc_slots(size_t n) {
   TRY(dalloc(&rb_.hist, hn));
   TRY(dalloc(&rb_.part, scan_parts_needed(std::max<uint32_t>(hn, (uint32_t)na)) + 16));
   TRY(dalloc(&dbgF_, 3 * na)); TRY(dalloc(&dbgT_, 3 * na));
+  TRY(dalloc(&aorder_, na)); TRY(dalloc(&wq_, na)); TRY(dalloc(&wcand_, na * WALL_CAND_CAP));
   TRY(dalloc(&ccnt_, na)); TRY(dalloc(&ncomp_, na)); TRY(dalloc(&coff_, na)); TRY(dalloc(&poff_, na));
   TRY(dalloc(&nnet_, na)); TRY(dalloc(&noff_, na));
-  TRY(dalloc(&ctot_, 4)); TRY(dalloc(&cpart_, scan_parts_needed((uint32_t)na) + 16));
-  CK(cudaMemset(ctot_, 0, 4 * sizeof(uint32_t)));
+  TRY(dalloc(&ctot_, 8)); TRY(dalloc(&cpart_, scan_parts_needed((uint32_t)na) + 16));
+  CK(cudaMemset(ctot_, 0, 8 * sizeof(uint32_t)));
   n_alloc_ = na;
   // lists must be re-allocated for the new slot count
   for (int b = 0; b < 2; ++b) {
@@ -409,6 +450,9 @@ void Engine::refresh_list_ptrs() {
   P_.clist = clist_;
   P_.cres = cres_;
   P_.ccnt = ccnt_;
+  P_.aorder = aorder_;
+  P_.wq = wq_;
+  P_.wcand = wcand_;
   P_.ncomp = ncomp_;
   P_.coff = coff_;
   P_.poff = poff_;
@@ -434,6 +478,7 @@ int Engine::build_params() {
     P.bmin[k] = bmin[k];
     P.bmax[k] = bmax[k];
     P.bsize[k] = bmax[k] - bmin[k];
+    P.bsizef[k] = (float)P.bsize[k];
     P.gravity[k] = gravity[k];
   }
   P.pm = pm;
@@ -621,7 +666,8 @@ int Engine::build_triangle_grid(double rmax) {
     }
   }
   double ext = std::max(hi[0] - lo[0], std::max(hi[1] - lo[1], hi[2] - lo[2]));
-  double cell = std::max(2.0 * rmax, ext / 1024.0);
+  // cells of about a radius keep the per-cell lists (pruned by distance below) short
+  double cell = std::max(rmax, ext / 1024.0);
   if (!(cell > 0.0)) cell = 1.0;
   std::vector<uint32_t> counts;
   int dims[3];
@@ -651,15 +697,31 @@ int Engine::build_triangle_grid(double rmax) {
   }
   const size_t nc = (size_t)dims[0] * dims[1] * dims[2];
   std::vector<uint32_t> start(nc + 1, 0);
+  // A triangle is listed in the cells of its grown box whose centre lies
+  // within half a cell diagonal plus the growth of the triangle itself: a
+  // centre that rounds into such a cell and lies within rmax of the triangle
+  // is within that distance of the cell's centre (degenerate triangles keep
+  // the whole box).
+  const double reach = cell * std::sqrt(3.0) * 0.5 + grow;
+  const double reach2 = reach * reach * (1.0 + 1e-9) + 1e-24;
   auto for_cells = [&](size_t t, auto&& f) {
     int a[3], b[3];
     for (int k = 0; k < 3; ++k) {
       a[k] = std::max(0, (int)std::floor((blo[3 * t + k] - lo[k]) / cell));
       b[k] = std::min(dims[k] - 1, (int)std::floor((bhi[3 * t + k] - lo[k]) / cell));
     }
+    const float* q = &tri_v_[9 * t];
+    const double v0[3] = {q[0], q[1], q[2]}, v1[3] = {q[3], q[4], q[5]}, v2[3] = {q[6], q[7], q[8]};
+    const bool flat = recs[t].plane.x == 0.f && recs[t].plane.y == 0.f && recs[t].plane.z == 0.f;
     for (int z = a[2]; z <= b[2]; ++z)
       for (int y = a[1]; y <= b[1]; ++y)
-        for (int x = a[0]; x <= b[0]; ++x) f((size_t)x + (size_t)dims[0] * ((size_t)y + (size_t)dims[1] * z));
+        for (int x = a[0]; x <= b[0]; ++x) {
+          if (!flat) {
+            const double cc[3] = {lo[0] + (x + 0.5) * cell, lo[1] + (y + 0.5) * cell, lo[2] + (z + 0.5) * cell};
+            if (point_triangle_dist2(cc, v0, v1, v2) > reach2) continue;  // NaN keeps the cell
+          }
+          f((size_t)x + (size_t)dims[0] * ((size_t)y + (size_t)dims[1] * z));
+        }
   };
   for (size_t t = 0; t < T; ++t) for_cells(t, [&](size_t c) { start[c + 1]++; });
   for (size_t c = 0; c < nc; ++c) start[c + 1] += start[c];
@@ -737,6 +799,9 @@ int Engine::upload() {
     for (size_t i = 0; i < n; ++i)
       xref[i] = make_float4((float)hp_[i].x[0], (float)hp_[i].x[1], (float)hp_[i].x[2], (float)hp_[i].r);
     CK(cudaMemcpy(B.xf, xref.data(), sizeof(float4) * n, cudaMemcpyHostToDevice));
+    std::vector<uint32_t> iota(n);  // replaced by the first list rebuild
+    for (size_t i = 0; i < n; ++i) iota[i] = (uint32_t)i;
+    CK(cudaMemcpy(aorder_, iota.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice));
   }
   for (int b = 0; b < 2; ++b) CK(cudaMemset(bank_[b].ncnt, 0, sizeof(uint32_t) * n_alloc_));
   if (need_hist)

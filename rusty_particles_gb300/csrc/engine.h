@@ -136,6 +136,9 @@ class Engine {
   // contact-parallel force buffers
   CRec* crec_ = nullptr;
   uint32_t *ccnt_ = nullptr, *ncomp_ = nullptr, *coff_ = nullptr, *poff_ = nullptr, *clist_ = nullptr;
+  uint32_t* aorder_ = nullptr;  // k_accumulate visiting order (set at every list rebuild)
+  uint2* wq_ = nullptr;         // wall queue of the accumulate pass
+  uint32_t* wcand_ = nullptr;   // wall candidates per slot
   uint32_t *ctot_ = nullptr, *cpart_ = nullptr;
   double* cres_ = nullptr;
   void refresh_list_ptrs();

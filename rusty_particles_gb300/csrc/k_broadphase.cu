@@ -362,9 +362,9 @@ __global__ void k_build_nlist(StepParams P, const uint32_t* cstart, const uint32
             // 2.5e-7 (2X + L) + a relative 1e-5 keeps the list a superset
             const float4 xj = B.xf[j];
             float fx = xif.x - xj.x, fy = xif.y - xj.y, fz = xif.z - xj.z;
-            if (P.periodic[0]) fx -= (float)P.bsize[0] * rintf(fx / (float)P.bsize[0]);
-            if (P.periodic[1]) fy -= (float)P.bsize[1] * rintf(fy / (float)P.bsize[1]);
-            if (P.periodic[2]) fz -= (float)P.bsize[2] * rintf(fz / (float)P.bsize[2]);
+            if (P.periodic[0]) fx -= P.bsizef[0] * rintf(fx / P.bsizef[0]);
+            if (P.periodic[1]) fy -= P.bsizef[1] * rintf(fy / P.bsizef[1]);
+            if (P.periodic[2]) fz -= P.bsizef[2] * rintf(fz / P.bsizef[2]);
             float d2 = fx * fx + fy * fy + fz * fz;
             const float X = fmaxf(Xi, fmaxf(fmaxf(fabsf(xj.x), fabsf(xj.y)), fabsf(xj.z)));
             float rl = (ri + xj.w) * adh + skin;
@@ -421,8 +421,9 @@ int launch_rebuild(const StepParams& P, const RebuildBufs& R, cudaStream_t s) {
   k_cell_bounds<<<nb, 256, 0, s>>>(g, sk, (uint32_t)P.n, P.fncells, R.cstart, R.cend);
   k_reorder<<<nb, 256, 0, s>>>(P, sv);
   k_build_nlist<<<grid_for(P.n, 128), 128, 0, s>>>(P, R.cstart, R.cend, sv, R.carry_history);
+  const int ko = launch_accum_order(P, s);
   k_rebuild_finish<<<1, 1, 0, s>>>(P);
-  return 1 + 5 * passes + 5;
+  return 1 + 5 * passes + 5 + ko;
 }
 
 // Diagnostic: the reference grid's key per slot (written to kraw) and the

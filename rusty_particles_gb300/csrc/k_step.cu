@@ -524,9 +524,9 @@ __global__ void __launch_bounds__(256) k_first_half(StepParams P) {
     B.xf[k] = xf;
     float4 r0 = B.xref[k];
     float ddx = xf.x - r0.x, ddy = xf.y - r0.y, ddz = xf.z - r0.z;
-    if (P.periodic[0]) ddx -= (float)P.bsize[0] * rintf(ddx / (float)P.bsize[0]);
-    if (P.periodic[1]) ddy -= (float)P.bsize[1] * rintf(ddy / (float)P.bsize[1]);
-    if (P.periodic[2]) ddz -= (float)P.bsize[2] * rintf(ddz / (float)P.bsize[2]);
+    if (P.periodic[0]) ddx -= P.bsizef[0] * rintf(ddx / P.bsizef[0]);
+    if (P.periodic[1]) ddy -= P.bsizef[1] * rintf(ddy / P.bsizef[1]);
+    if (P.periodic[2]) ddz -= P.bsizef[2] * rintf(ddz / P.bsizef[2]);
     float d2 = ddx * ddx + ddy * ddy + ddz * ddz;
     if (!(d2 <= half_skin * half_skin)) want_rebuild = true;  // NaN (no build yet) also rebuilds
   }
@@ -560,95 +560,121 @@ __global__ void __launch_bounds__(256) k_second_half(StepParams P) {
 // plane is farther than the radius (plus rounding) cannot touch the sphere,
 // because the closest point lies in that plane: both skip FP64 work only.
 // Triangles of another group than the particle's (gi) are not walls for it.
+
+// The triangle-grid cell of an FP32 position: its range of triangle entries,
+// or false outside the grid.
+__device__ __forceinline__ bool tri_cell_range(const StepParams& P, float4 xf, uint32_t& s, uint32_t& e) {
+  const float q0 = floorf((xf.x - P.tminf[0]) * P.tinvf);
+  const float q1 = floorf((xf.y - P.tminf[1]) * P.tinvf);
+  const float q2 = floorf((xf.z - P.tminf[2]) * P.tinvf);
+  if (!(q0 >= 0.f && q1 >= 0.f && q2 >= 0.f && q0 < (float)P.tdims[0] && q1 < (float)P.tdims[1] &&
+        q2 < (float)P.tdims[2]))
+    return false;
+  const uint32_t cell = (uint32_t)q0 + (uint32_t)P.tdims[0] * ((uint32_t)q1 + (uint32_t)P.tdims[1] * (uint32_t)q2);
+  s = P.tstart[cell];
+  e = P.tstart[cell + 1];
+  return true;
+}
+
+// FP32 pretest of a sphere (centre xf, radius rf = xf.w, largest |coordinate|
+// xmag, group gi) against a triangle: false when it cannot touch it.
+__device__ __forceinline__ bool wall_pretest(const TriRec& tr, uint32_t gi, float4 xf, float xmag) {
+  if (tr.group != GROUP_ALL && tr.group != gi) return false;
+  const float rf = xf.w;
+  // FP32 rounding of n, n.v0 and x moves n.x - n.v0 by at most
+  // ~3e-7 (|x| + |n.v0|) + 1.1e-7 |x - v0|; the margin is larger
+  const float4 pl = tr.plane;
+  const float hd = fabsf(pl.x * xf.x + pl.y * xf.y + pl.z * xf.z - pl.w);
+  const float mrg = 1e-6f * (1.0f + xmag + fabsf(pl.w) + rf) + 2e-7f * (xmag + tr.bound.x);
+  if (hd > rf + mrg) return false;
+  // the distance to the triangle is at least sqrt(hd^2 + s^2), s the
+  // largest outward in-plane distance to an edge line (each with the
+  // plane test's rounding margin; |m.v| <= sqrt(3) bound)
+  const float4 g0 = tr.edge[0], g1 = tr.edge[1], g2 = tr.edge[2];
+  const float s = fmaxf(fmaxf(g0.x * xf.x + g0.y * xf.y + g0.z * xf.z - g0.w,
+                              g1.x * xf.x + g1.y * xf.y + g1.z * xf.z - g1.w),
+                        g2.x * xf.x + g2.y * xf.y + g2.z * xf.z - g2.w);
+  const float me = mrg + 4e-7f * tr.bound.x;
+  const float hl = fmaxf(hd - mrg, 0.0f), sl = fmaxf(s - me, 0.0f);
+  return !(hl * hl + sl * sl > rf * rf * (1.0f + 1e-6f));
+}
+
+// The FP64 contact of a sphere with a triangle that passed the pretest:
+// force fc and torque r_a x fc on the sphere, or false (outputs untouched)
+// when it does not touch the triangle.
+__device__ __forceinline__ bool wall_contact(const StepParams& P, const Law& L, const TriRec& tr, V xi, V vi, V wi,
+                                             double ri, double mi, V& fc_out, V& tc_out, bool& excess) {
+  // closest point, src/mesh.rs:45-117 (same regions and clamps)
+  const V v0 = vmk(tr.v0[0] - xi.x, tr.v0[1] - xi.y, tr.v0[2] - xi.z);
+  const V e0 = vmk(tr.e0[0], tr.e0[1], tr.e0[2]), e1 = vmk(tr.e1[0], tr.e1[1], tr.e1[2]);
+  const double a = tr.a, b = tr.b, c = tr.c, det = tr.det;
+  const double dd = dot(e0, v0), ee = dot(e1, v0);
+  const double s0 = b * ee - c * dd, t0 = b * dd - a * ee;
+  double sc = s0, tc = t0;
+  if (s0 + t0 < det) {
+    if (s0 < 0.0) {
+      if (t0 < 0.0) {
+        if (dd < 0.0) { sc = fmin(fmax(-dd, 0.0), a); tc = 0.0; }
+        else { sc = 0.0; tc = fmin(fmax(-ee, 0.0), c); }
+      } else { sc = 0.0; tc = fmin(fmax(-ee, 0.0), c); }
+    } else if (t0 < 0.0) {
+      sc = fmin(fmax(-dd, 0.0), a); tc = 0.0;
+    } else {
+      const double inv = 1.0 / det;
+      sc = sc * inv; tc = tc * inv;
+    }
+  } else {
+    if (s0 < 0.0) {
+      const double tmp0 = b + dd, tmp1 = c + ee;
+      if (tmp1 > tmp0) {
+        const double numer = tmp1 - tmp0;
+        sc = numer / tr.denom; sc = sc < 0.0 ? 0.0 : (sc > 1.0 ? 1.0 : sc); tc = 1.0 - sc;
+      } else { tc = fmin(fmax(-ee, 0.0), c); sc = 0.0; }
+    } else if (t0 < 0.0) {
+      if (a + dd > b + ee) {
+        const double numer = c + ee - b - dd;
+        sc = numer / tr.denom; sc = sc < 0.0 ? 0.0 : (sc > 1.0 ? 1.0 : sc); tc = 1.0 - sc;
+      } else { sc = fmin(fmax(-ee, 0.0), c); tc = 0.0; }
+    } else {
+      const double numer = c + ee - b - dd;
+      sc = numer / tr.denom; sc = sc < 0.0 ? 0.0 : (sc > 1.0 ? 1.0 : sc); tc = 1.0 - sc;
+    }
+  }
+  const V cp = vmk(tr.v0[0], tr.v0[1], tr.v0[2]) + sc * e0 + tc * e1;
+  const V dv = xi - cp;
+  const double dsq = dot(dv, dv);
+  if (!(dsq < ri * ri)) return false;
+  const double dist = sqrt(dsq);
+  const double pen = ri - dist;
+  const V n = dist > 1e-6 ? dv / dist : vmk(tr.n[0], tr.n[1], tr.n[2]);
+  if (pen > 0.2 * ri) excess = true;
+  const V ra = (-n) * ri;
+  V rv = vi + cross(wi, ra);
+  if (tr.motion != NO_MOTION) {  // a moving wall: relative to its surface velocity at the contact point
+    const WallMotion& M = P.motions[tr.motion];
+    const V vw = vmk(M.v[0], M.v[1], M.v[2]) + cross(vmk(M.w[0], M.w[1], M.w[2]), cp - vmk(M.c[0], M.c[1], M.c[2]));
+    rv = rv - vw;
+  }
+  const V fnv = normal_force<double>(P.nmodel, pen, n, rv, L.es_pw, ri, mi, L.beta_abs, L.gamma_pw, true);
+  const V fc = fnv + coulomb_force<double>(len(fnv), rv, n, L.mu);
+  fc_out = fc;
+  tc_out = cross(ra, fc);
+  return true;
+}
+
+// All wall contacts of one particle in mesh order.
 __device__ __forceinline__ void wall_forces(const StepParams& P, const Law& L, uint32_t gi, V xi, float4 xf, V vi,
                                             V wi, double ri, double mi, V& F, V& T, bool& excess) {
-  if (P.ntri > 0) {
-    const float q0 = floorf((xf.x - P.tminf[0]) * P.tinvf);
-    const float q1 = floorf((xf.y - P.tminf[1]) * P.tinvf);
-    const float q2 = floorf((xf.z - P.tminf[2]) * P.tinvf);
-    if (q0 >= 0.f && q1 >= 0.f && q2 >= 0.f && q0 < (float)P.tdims[0] && q1 < (float)P.tdims[1] &&
-        q2 < (float)P.tdims[2]) {
-      const uint32_t cell = (uint32_t)q0 + (uint32_t)P.tdims[0] * ((uint32_t)q1 + (uint32_t)P.tdims[1] * (uint32_t)q2);
-      const uint32_t s = P.tstart[cell], e = P.tstart[cell + 1];
-      const float rf = (float)ri;
-      const float xmag = fmaxf(fmaxf(fabsf(xf.x), fabsf(xf.y)), fabsf(xf.z));
-      for (uint32_t t = s; t < e; ++t) {
-        const TriRec& tr = P.tri[P.titems[t]];
-        if (tr.group != GROUP_ALL && tr.group != gi) continue;
-        // FP32 rounding of n, n.v0 and x moves n.x - n.v0 by at most
-        // ~3e-7 (|x| + |n.v0|) + 1.1e-7 |x - v0|; the margin is larger
-        const float4 pl = tr.plane;
-        const float hd = fabsf(pl.x * xf.x + pl.y * xf.y + pl.z * xf.z - pl.w);
-        const float mrg = 1e-6f * (1.0f + xmag + fabsf(pl.w) + rf) + 2e-7f * (xmag + tr.bound.x);
-        if (hd > rf + mrg) continue;
-        // the distance to the triangle is at least sqrt(hd^2 + s^2), s the
-        // largest outward in-plane distance to an edge line (each with the
-        // plane test's rounding margin; |m.v| <= sqrt(3) bound)
-        {
-          const float4 g0 = tr.edge[0], g1 = tr.edge[1], g2 = tr.edge[2];
-          const float s = fmaxf(fmaxf(g0.x * xf.x + g0.y * xf.y + g0.z * xf.z - g0.w,
-                                      g1.x * xf.x + g1.y * xf.y + g1.z * xf.z - g1.w),
-                                g2.x * xf.x + g2.y * xf.y + g2.z * xf.z - g2.w);
-          const float me = mrg + 4e-7f * tr.bound.x;
-          const float hl = fmaxf(hd - mrg, 0.0f), sl = fmaxf(s - me, 0.0f);
-          if (hl * hl + sl * sl > rf * rf * (1.0f + 1e-6f)) continue;
-        }
-        // closest point, src/mesh.rs:45-117 (same regions and clamps)
-        const V v0 = vmk(tr.v0[0] - xi.x, tr.v0[1] - xi.y, tr.v0[2] - xi.z);
-        const V e0 = vmk(tr.e0[0], tr.e0[1], tr.e0[2]), e1 = vmk(tr.e1[0], tr.e1[1], tr.e1[2]);
-        const double a = tr.a, b = tr.b, c = tr.c, det = tr.det;
-        const double dd = dot(e0, v0), ee = dot(e1, v0);
-        const double s0 = b * ee - c * dd, t0 = b * dd - a * ee;
-        double sc = s0, tc = t0;
-        if (s0 + t0 < det) {
-          if (s0 < 0.0) {
-            if (t0 < 0.0) {
-              if (dd < 0.0) { sc = fmin(fmax(-dd, 0.0), a); tc = 0.0; }
-              else { sc = 0.0; tc = fmin(fmax(-ee, 0.0), c); }
-            } else { sc = 0.0; tc = fmin(fmax(-ee, 0.0), c); }
-          } else if (t0 < 0.0) {
-            sc = fmin(fmax(-dd, 0.0), a); tc = 0.0;
-          } else {
-            const double inv = 1.0 / det;
-            sc = sc * inv; tc = tc * inv;
-          }
-        } else {
-          if (s0 < 0.0) {
-            const double tmp0 = b + dd, tmp1 = c + ee;
-            if (tmp1 > tmp0) {
-              const double numer = tmp1 - tmp0;
-              sc = numer / tr.denom; sc = sc < 0.0 ? 0.0 : (sc > 1.0 ? 1.0 : sc); tc = 1.0 - sc;
-            } else { tc = fmin(fmax(-ee, 0.0), c); sc = 0.0; }
-          } else if (t0 < 0.0) {
-            if (a + dd > b + ee) {
-              const double numer = c + ee - b - dd;
-              sc = numer / tr.denom; sc = sc < 0.0 ? 0.0 : (sc > 1.0 ? 1.0 : sc); tc = 1.0 - sc;
-            } else { sc = fmin(fmax(-ee, 0.0), c); tc = 0.0; }
-          } else {
-            const double numer = c + ee - b - dd;
-            sc = numer / tr.denom; sc = sc < 0.0 ? 0.0 : (sc > 1.0 ? 1.0 : sc); tc = 1.0 - sc;
-          }
-        }
-        const V cp = vmk(tr.v0[0], tr.v0[1], tr.v0[2]) + sc * e0 + tc * e1;
-        const V dv = xi - cp;
-        const double dsq = dot(dv, dv);
-        if (!(dsq < ri * ri)) continue;
-        const double dist = sqrt(dsq);
-        const double pen = ri - dist;
-        const V n = dist > 1e-6 ? dv / dist : vmk(tr.n[0], tr.n[1], tr.n[2]);
-        if (pen > 0.2 * ri) excess = true;
-        const V ra = (-n) * ri;
-        V rv = vi + cross(wi, ra);
-        if (tr.motion != NO_MOTION) {  // a moving wall: relative to its surface velocity at the contact point
-          const WallMotion& M = P.motions[tr.motion];
-          const V vw = vmk(M.v[0], M.v[1], M.v[2]) + cross(vmk(M.w[0], M.w[1], M.w[2]), cp - vmk(M.c[0], M.c[1], M.c[2]));
-          rv = rv - vw;
-        }
-        const V fnv = normal_force<double>(P.nmodel, pen, n, rv, L.es_pw, ri, mi, L.beta_abs, L.gamma_pw, true);
-        const V fc = fnv + coulomb_force<double>(len(fnv), rv, n, L.mu);
-        F = F + fc;
-        T = T + cross(ra, fc);
-      }
+  uint32_t s, e;
+  if (P.ntri == 0 || !tri_cell_range(P, xf, s, e)) return;
+  const float xmag = fmaxf(fmaxf(fabsf(xf.x), fabsf(xf.y)), fabsf(xf.z));
+  for (uint32_t t = s; t < e; ++t) {
+    const TriRec& tr = P.tri[P.titems[t]];
+    if (!wall_pretest(tr, gi, xf, xmag)) continue;
+    V fc, tc;
+    if (wall_contact(P, L, tr, xi, vi, wi, ri, mi, fc, tc, excess)) {
+      F = F + fc;
+      T = T + tc;
     }
   }
 }
@@ -691,9 +717,9 @@ __global__ void __launch_bounds__(128) k_force(StepParams P) {
         // certainly outside and the exact FP64 test is skipped.
         const float4 xjf = B.xf[j];
         float fx = xif.x - xjf.x, fy = xif.y - xjf.y, fz = xif.z - xjf.z;
-        if (P.periodic[0]) { const float L = (float)P.bsize[0]; if (fx > 0.5f * L) fx -= L; else if (fx < -0.5f * L) fx += L; }
-        if (P.periodic[1]) { const float L = (float)P.bsize[1]; if (fy > 0.5f * L) fy -= L; else if (fy < -0.5f * L) fy += L; }
-        if (P.periodic[2]) { const float L = (float)P.bsize[2]; if (fz > 0.5f * L) fz -= L; else if (fz < -0.5f * L) fz += L; }
+        if (P.periodic[0]) { const float L = P.bsizef[0]; if (fx > 0.5f * L) fx -= L; else if (fx < -0.5f * L) fx += L; }
+        if (P.periodic[1]) { const float L = P.bsizef[1]; if (fy > 0.5f * L) fy -= L; else if (fy < -0.5f * L) fy += L; }
+        if (P.periodic[2]) { const float L = P.bsizef[2]; if (fz > 0.5f * L) fz -= L; else if (fz < -0.5f * L) fz += L; }
         const float d2f = fx * fx + fy * fy + fz * fz;
         const float rsf = xif.w + xjf.w;
         const float cutf = adh ? rsf * 1.5f : rsf;
@@ -776,9 +802,9 @@ __global__ void __launch_bounds__(128) k_force(StepParams P) {
 // larger band below the pair is certainly outside the exact FP64 test.
 __device__ __forceinline__ bool pretest_far(const StepParams& P, float4 xif, float Xi, float4 xjf, bool adh) {
   float fx = xif.x - xjf.x, fy = xif.y - xjf.y, fz = xif.z - xjf.z;
-  if (P.periodic[0]) { const float L = (float)P.bsize[0]; if (fx > 0.5f * L) fx -= L; else if (fx < -0.5f * L) fx += L; }
-  if (P.periodic[1]) { const float L = (float)P.bsize[1]; if (fy > 0.5f * L) fy -= L; else if (fy < -0.5f * L) fy += L; }
-  if (P.periodic[2]) { const float L = (float)P.bsize[2]; if (fz > 0.5f * L) fz -= L; else if (fz < -0.5f * L) fz += L; }
+  if (P.periodic[0]) { const float L = P.bsizef[0]; if (fx > 0.5f * L) fx -= L; else if (fx < -0.5f * L) fx += L; }
+  if (P.periodic[1]) { const float L = P.bsizef[1]; if (fy > 0.5f * L) fy -= L; else if (fy < -0.5f * L) fy += L; }
+  if (P.periodic[2]) { const float L = P.bsizef[2]; if (fz > 0.5f * L) fz -= L; else if (fz < -0.5f * L) fz += L; }
   const float d2f = fx * fx + fy * fy + fz * fz;
   const float rsf = xif.w + xjf.w;
   const float cutf = adh ? rsf * 1.5f : rsf;
@@ -802,9 +828,9 @@ __device__ __forceinline__ V mic(const StepParams& P, V d) {
 // reference's Newton.
 __device__ __forceinline__ bool jkr_net_hint(const StepParams& P, float Cf, float4 xif, float4 xjf) {
   float fx = xif.x - xjf.x, fy = xif.y - xjf.y, fz = xif.z - xjf.z;
-  if (P.periodic[0]) { const float L = (float)P.bsize[0]; if (fx > 0.5f * L) fx -= L; else if (fx < -0.5f * L) fx += L; }
-  if (P.periodic[1]) { const float L = (float)P.bsize[1]; if (fy > 0.5f * L) fy -= L; else if (fy < -0.5f * L) fy += L; }
-  if (P.periodic[2]) { const float L = (float)P.bsize[2]; if (fz > 0.5f * L) fz -= L; else if (fz < -0.5f * L) fz += L; }
+  if (P.periodic[0]) { const float L = P.bsizef[0]; if (fx > 0.5f * L) fx -= L; else if (fx < -0.5f * L) fx += L; }
+  if (P.periodic[1]) { const float L = P.bsizef[1]; if (fy > 0.5f * L) fy -= L; else if (fy < -0.5f * L) fy += L; }
+  if (P.periodic[2]) { const float L = P.bsizef[2]; if (fz > 0.5f * L) fz -= L; else if (fz < -0.5f * L) fz += L; }
   const float rsum = xif.w + xjf.w;
   const float rs = xif.w * xjf.w / rsum;
   const float c = Cf / rs;
@@ -830,9 +856,9 @@ __device__ __forceinline__ bool jkr_net_hint(const StepParams& P, float Cf, floa
 // bit for bit, so both ends of a pair drop it or keep it together.
 __device__ __forceinline__ bool jkr_far_zero(const StepParams& P, float Cf, float4 xif, float Xi, float4 xjf) {
   float fx = xif.x - xjf.x, fy = xif.y - xjf.y, fz = xif.z - xjf.z;
-  if (P.periodic[0]) { const float L = (float)P.bsize[0]; if (fx > 0.5f * L) fx -= L; else if (fx < -0.5f * L) fx += L; }
-  if (P.periodic[1]) { const float L = (float)P.bsize[1]; if (fy > 0.5f * L) fy -= L; else if (fy < -0.5f * L) fy += L; }
-  if (P.periodic[2]) { const float L = (float)P.bsize[2]; if (fz > 0.5f * L) fz -= L; else if (fz < -0.5f * L) fz += L; }
+  if (P.periodic[0]) { const float L = P.bsizef[0]; if (fx > 0.5f * L) fx -= L; else if (fx < -0.5f * L) fx += L; }
+  if (P.periodic[1]) { const float L = P.bsizef[1]; if (fy > 0.5f * L) fy -= L; else if (fy < -0.5f * L) fy += L; }
+  if (P.periodic[2]) { const float L = P.bsizef[2]; if (fz > 0.5f * L) fz -= L; else if (fz < -0.5f * L) fz += L; }
   const float rsum = xif.w + xjf.w;
   const float rs = (xif.w * xjf.w) / rsum;
   const float c = Cf / rs;
@@ -854,9 +880,9 @@ __device__ __forceinline__ bool jkr_far_zero(const StepParams& P, float Cf, floa
 // margin. Symmetric in (i, j) bit for bit.
 __device__ __forceinline__ bool sjkr_far_zero(const StepParams& P, const Law& L, float4 xif, float Xi, float4 xjf) {
   float fx = xif.x - xjf.x, fy = xif.y - xjf.y, fz = xif.z - xjf.z;
-  if (P.periodic[0]) { const float Lp = (float)P.bsize[0]; if (fx > 0.5f * Lp) fx -= Lp; else if (fx < -0.5f * Lp) fx += Lp; }
-  if (P.periodic[1]) { const float Lp = (float)P.bsize[1]; if (fy > 0.5f * Lp) fy -= Lp; else if (fy < -0.5f * Lp) fy += Lp; }
-  if (P.periodic[2]) { const float Lp = (float)P.bsize[2]; if (fz > 0.5f * Lp) fz -= Lp; else if (fz < -0.5f * Lp) fz += Lp; }
+  if (P.periodic[0]) { const float Lp = P.bsizef[0]; if (fx > 0.5f * Lp) fx -= Lp; else if (fx < -0.5f * Lp) fx += Lp; }
+  if (P.periodic[1]) { const float Lp = P.bsizef[1]; if (fy > 0.5f * Lp) fy -= Lp; else if (fy < -0.5f * Lp) fy += Lp; }
+  if (P.periodic[2]) { const float Lp = P.bsizef[2]; if (fz > 0.5f * Lp) fz -= Lp; else if (fz < -0.5f * Lp) fz += Lp; }
   const float rsum = xif.w + xjf.w;
   const float rs = (xif.w * xjf.w) / rsum;
   const float d = sqrtf(fx * fx + fy * fy + fz * fz);
@@ -892,7 +918,10 @@ __global__ void __launch_bounds__(256) k_contact_filter(StepParams P) {
   // the same for sJKR, whose zero region is explicit (no iteration to certify)
   const bool sdrop = P.nmodel == 4 && P.pretest && !P.debug && (P.tmodel == 0 || PHYS);
   const size_t plane = (size_t)P.n * P.cap;
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < P.n; k += gridDim.x * blockDim.x) {
+  // slots in the rebuild-time order (tiles of 256 sorted by list length), so
+  // a warp's lanes walk lists of similar length
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n; i += gridDim.x * blockDim.x) {
+    const int k = (int)P.aorder[i];
     uint32_t nrec = 0, ncmp = 0, nnet = 0;
     if (!(B.flags[k] & PF_DEAD)) {
       const unsigned long long ci = PHYS ? 0ull : (unsigned long long)__double_as_longlong(B.wc[k].w);
@@ -947,7 +976,10 @@ __global__ void __launch_bounds__(256) k_contact_filter(StepParams P) {
 __global__ void __launch_bounds__(256) k_contact_index(StepParams P) {
   if (P.ctrl->halt) return;
   const bool learn = P.jkr_solver == 1 && P.nmodel == 3 && P.mlp != nullptr;
-  if (blockIdx.x == 0 && threadIdx.x == 0) P.ctot[3] = 0u;  // deferred pairs of this step
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    P.ctot[3] = 0u;  // deferred pairs of this step
+    P.ctot[4] = 0u;  // particles queued for k_accumulate_walls
+  }
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < P.n; k += gridDim.x * blockDim.x) {
     const uint32_t n = P.ccnt[k];
     uint32_t q = P.poff[k];
@@ -1166,90 +1198,260 @@ __global__ void __launch_bounds__(128) k_contact_deferred(StepParams P) {
 }
 
 // Pass 4: per particle, the contact results in list order, the walls, then
-// a = g + F/m and tau = T (src/simulation.rs:265-271, 532-536).
-// Threads take their block's particles in the order of a shared-memory
-// counting sort by (triangles listed in the particle's cell, contact count),
-// so a warp's lanes run loops of similar length; each particle's arithmetic
-// is the same whatever thread runs it.
+// a = g + F/m and tau = T (src/simulation.rs:265-271, 532-536), in two
+// kernels. k_accumulate (few registers, many warps in flight for the loads)
+// sums the contact results of every particle and finishes those whose
+// triangle-grid cell lists no triangle; the others are queued with their
+// partial F and T, and k_accumulate_walls adds their wall contacts: FP32
+// pretests per particle, then the block's (particle, triangle) candidates
+// evaluated densely, one per thread per round, with results in shared
+// memory; each particle adds its own in mesh order, so F and T are the same
+// sums as one thread walking its triangles. k_accumulate takes the slots in
+// the order P.aorder, set at each list rebuild, so that a warp's lanes run
+// loops of similar length; no order changes a result.
 constexpr uint32_t ACC_BINS = 128;
+constexpr uint32_t ACC_TILE = 256;
 
 __device__ __forceinline__ bool tri_cell_nonempty(const StepParams& P, float4 xf) {
-  const float q0 = floorf((xf.x - P.tminf[0]) * P.tinvf);
-  const float q1 = floorf((xf.y - P.tminf[1]) * P.tinvf);
-  const float q2 = floorf((xf.z - P.tminf[2]) * P.tinvf);
-  if (!(q0 >= 0.f && q1 >= 0.f && q2 >= 0.f && q0 < (float)P.tdims[0] && q1 < (float)P.tdims[1] &&
-        q2 < (float)P.tdims[2]))
-    return false;
-  const uint32_t cell = (uint32_t)q0 + (uint32_t)P.tdims[0] * ((uint32_t)q1 + (uint32_t)P.tdims[1] * (uint32_t)q2);
-  return P.tstart[cell + 1] > P.tstart[cell];
+  uint32_t s, e;
+  return tri_cell_range(P, xf, s, e) && e > s;
+}
+
+// The visiting order of k_accumulate, at a list rebuild: within each tile of
+// 256 slots a counting sort by (triangles listed in the triangle-grid cell,
+// Verlet-list length), dead slots after the live ones. Reads the bank the
+// rebuild fills.
+__global__ void __launch_bounds__(ACC_TILE) k_accum_order(StepParams P) {
+  {
+    volatile const Ctrl* c = P.ctrl;
+    if (c->rebuild == 0 || c->halt != 0) return;
+  }
+  const Bank B = P.bank[P.ctrl->bank ^ 1];
+  __shared__ uint32_t bins[ACC_BINS];
+  for (int base = blockIdx.x * ACC_TILE; base < P.n; base += gridDim.x * ACC_TILE) {
+    const int k0 = base + threadIdx.x;
+    // keys: 0..62 no triangles, 63 dead, 64..126 triangles, 127 past the end
+    uint32_t key = ACC_BINS - 1;
+    if (k0 < P.n) {
+      if (B.flags[k0] & PF_DEAD) {
+        key = 63;
+      } else {
+        key = min(B.ncnt[k0], 62u);
+        if (P.ntri > 0 && tri_cell_nonempty(P, B.xf[k0])) key += 64;
+      }
+    }
+    for (uint32_t i = threadIdx.x; i < ACC_BINS; i += blockDim.x) bins[i] = 0;
+    __syncthreads();
+    const uint32_t rank = atomicAdd(&bins[key], 1u);
+    __syncthreads();
+    if (threadIdx.x < 32) {  // exclusive scan of the bins, four per lane
+      const uint32_t l = threadIdx.x;
+      const uint32_t c0 = bins[4 * l], c1 = bins[4 * l + 1], c2 = bins[4 * l + 2], c3 = bins[4 * l + 3];
+      const uint32_t sum = c0 + c1 + c2 + c3;
+      uint32_t incl = sum;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (l >= (uint32_t)o) incl += t;
+      }
+      const uint32_t ex = incl - sum;
+      bins[4 * l] = ex;
+      bins[4 * l + 1] = ex + c0;
+      bins[4 * l + 2] = ex + c0 + c1;
+      bins[4 * l + 3] = ex + c0 + c1 + c2;
+    }
+    __syncthreads();
+    if (k0 < P.n) P.aorder[base + bins[key] + rank] = (uint32_t)k0;
+    __syncthreads();
+  }
+}
+
+int launch_accum_order(const StepParams& P, cudaStream_t s) {
+  const uint64_t tiles = ((uint64_t)P.n + ACC_TILE - 1) / ACC_TILE;
+  k_accum_order<<<(int)std::min<uint64_t>(std::max<uint64_t>(tiles, 1), 152ull * 64ull), ACC_TILE, 0, s>>>(P);
+  return 1;
+}
+
+// Exclusive scan of one value per thread (blockDim.x a multiple of 32, at
+// most 256); the block total goes to *total. Contains two __syncthreads.
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* wsum, uint32_t* total) {
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  uint32_t inc = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= (uint32_t)o) inc += t;
+  }
+  if (lane == 31) wsum[warp] = inc;
+  __syncthreads();
+  if (warp == 0) {
+    const uint32_t w = lane < nw ? wsum[lane] : 0u;
+    uint32_t wi = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xffffffffu, wi, o);
+      if (lane >= (uint32_t)o) wi += t;
+    }
+    if (lane < nw) wsum[lane] = wi - w;
+    if (lane == nw - 1) *total = wi;
+  }
+  __syncthreads();
+  return inc - v + wsum[warp];
+}
+
+// a = g + F (1/m) and tau = 0 + T for one particle, with the debug record and
+// the non-finite check (on the integer pipe, as the +0 of 0 + T).
+__device__ __forceinline__ void finish_particle(const StepParams& P, const Bank& B, Ctrl* C, int k, V F, V T) {
+  if (P.debug) {
+    P.dbgF[3 * (size_t)k] = F.x; P.dbgF[3 * (size_t)k + 1] = F.y; P.dbgF[3 * (size_t)k + 2] = F.z;
+    P.dbgT[3 * (size_t)k] = T.x; P.dbgT[3 * (size_t)k + 1] = T.y; P.dbgT[3 * (size_t)k + 2] = T.z;
+  }
+  if (!(finite_bits(F.x) & finite_bits(F.y) & finite_bits(F.z) & finite_bits(T.x) & finite_bits(T.y) &
+        finite_bits(T.z)))
+    atomicOr(&C->status, (unsigned)ST_NAN);
+  const V a = vmk(P.gravity[0], P.gravity[1], P.gravity[2]) + F * B.vres[k].w;  // F (1/m)
+  B.acc[k] = D4{a.x, a.y, a.z, 0.0};
+  B.tq[k] = D4{plus_zero(T.x), plus_zero(T.y), plus_zero(T.z), 0.0};
 }
 
 __global__ void __launch_bounds__(256) k_accumulate(StepParams P) {
   Ctrl* C = P.ctrl;
   if (C->halt) return;
   const Bank B = P.bank[C->bank];
-  __shared__ uint32_t bins[ACC_BINS];
-  __shared__ uint16_t order[256];
-  bool excess = false;
-  for (int base = blockIdx.x * blockDim.x; base < P.n; base += gridDim.x * blockDim.x) {
-    {
-      const int k0 = base + threadIdx.x;
-      uint32_t key = ACC_BINS - 1;
-      if (k0 < P.n && !(B.flags[k0] & PF_DEAD)) {
-        key = min(P.ccnt[k0], 63u);
-        if (P.ntri > 0 && tri_cell_nonempty(P, B.xf[k0])) key += 64;
-      }
-      for (uint32_t i = threadIdx.x; i < ACC_BINS; i += blockDim.x) bins[i] = 0;
-      __syncthreads();
-      const uint32_t rank = atomicAdd(&bins[key], 1u);
-      __syncthreads();
-      if (threadIdx.x < 32) {  // exclusive scan of the bins, four per lane
-        const uint32_t l = threadIdx.x;
-        const uint32_t c0 = bins[4 * l], c1 = bins[4 * l + 1], c2 = bins[4 * l + 2], c3 = bins[4 * l + 3];
-        const uint32_t sum = c0 + c1 + c2 + c3;
-        uint32_t incl = sum;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
-          if (l >= (uint32_t)o) incl += t;
-        }
-        const uint32_t ex = incl - sum;
-        bins[4 * l] = ex;
-        bins[4 * l + 1] = ex + c0;
-        bins[4 * l + 2] = ex + c0 + c1;
-        bins[4 * l + 3] = ex + c0 + c1 + c2;
-      }
-      __syncthreads();
-      order[bins[key] + rank] = (uint16_t)threadIdx.x;
-      __syncthreads();
-    }
-    const int k = base + order[threadIdx.x];
-    __syncthreads();  // order and bins are rewritten for the next tile
-    if (k >= P.n || (B.flags[k] & PF_DEAD)) continue;
+  const int lane = threadIdx.x & 31;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n; i += gridDim.x * blockDim.x) {
+    const int k = (int)P.aorder[i];
+    if (B.flags[k] & PF_DEAD) continue;
     V F = vmk(0.0, 0.0, 0.0), T = vmk(0.0, 0.0, 0.0);
     const uint32_t n = P.ccnt[k];
-    const double* res = P.cres + 6 * (size_t)P.coff[k];
+    const double2* res = reinterpret_cast<const double2*>(P.cres + 6 * (size_t)P.coff[k]);
     for (uint32_t c = 0; c < n; ++c) {
-      F = F + vmk(res[6 * c], res[6 * c + 1], res[6 * c + 2]);
-      T = T + vmk(res[6 * c + 3], res[6 * c + 4], res[6 * c + 5]);
+      const double2 r0 = res[3 * c], r1 = res[3 * c + 1], r2 = res[3 * c + 2];
+      F = F + vmk(r0.x, r0.y, r1.x);
+      T = T + vmk(r1.y, r2.x, r2.y);
     }
+    // wall pretests: the first WALL_CAND_CAP triangles that pass are kept
+    // for k_accumulate_walls (a count above the cap says there are more)
+    uint32_t nc = 0;
     if (P.ntri > 0) {
+      const float4 xf = B.xf[k];
+      uint32_t s, e;
+      if (tri_cell_range(P, xf, s, e) && e > s) {
+        const float xmag = fmaxf(fmaxf(fabsf(xf.x), fabsf(xf.y)), fabsf(xf.z));
+        const uint32_t gi = P.ngroups > 1 ? B.grp[k] : 0u;
+        uint32_t* out = P.wcand + (size_t)k * WALL_CAND_CAP;
+        for (uint32_t t = s; t < e; ++t) {
+          const uint32_t id = P.titems[t];
+          if (!wall_pretest(P.tri[id], gi, xf, xmag)) continue;
+          if (nc == WALL_CAND_CAP) {
+            ++nc;
+            break;
+          }
+          out[nc++] = id;
+        }
+      }
+    }
+    const bool walls = nc > 0;
+    // queue the particles with wall candidates, one atomic per warp
+    const unsigned act = __activemask();
+    const unsigned bal = __ballot_sync(act, walls);
+    if (bal) {
+      const int leader = __ffs(bal) - 1;
+      uint32_t q = 0;
+      if (lane == leader) q = atomicAdd(P.ctot + 4, (uint32_t)__popc(bal));
+      q = __shfl_sync(act, q, leader);
+      if (walls) P.wq[q + (uint32_t)__popc(bal & ((1u << lane) - 1u))] = make_uint2((uint32_t)k, nc);
+    }
+    if (walls) {  // partial sums, completed by k_accumulate_walls
+      B.acc[k] = D4{F.x, F.y, F.z, 0.0};
+      B.tq[k] = D4{T.x, T.y, T.z, 0.0};
+    } else {
+      finish_particle(P, B, C, k, F, T);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) k_accumulate_walls(StepParams P) {
+  Ctrl* C = P.ctrl;
+  if (C->halt) return;
+  const Bank B = P.bank[C->bank];
+  const uint32_t total = P.ctot[4];
+  __shared__ uint32_t kslot[256];  // the slot each thread of the tile took
+  __shared__ uint32_t woff[257];   // per-thread candidate offsets, then the block total
+  __shared__ uint32_t wsum[8];
+  __shared__ double wres[6][256];  // one round of dense results (force, torque)
+  __shared__ uint8_t wok[256];
+  bool excess = false;
+  for (uint32_t base = blockIdx.x * blockDim.x; base < total; base += gridDim.x * blockDim.x) {
+    const uint32_t i = base + threadIdx.x;
+    const bool live = i < total;
+    const uint2 qe = live ? P.wq[i] : make_uint2(0u, 0u);
+    const int k = (int)qe.x;
+    const uint32_t nc = min(qe.y, WALL_CAND_CAP);
+    V F = vmk(0.0, 0.0, 0.0), T = vmk(0.0, 0.0, 0.0);
+    if (live) {
+      F = xyz(B.acc[k]);
+      T = xyz(B.tq[k]);
+    }
+    kslot[threadIdx.x] = (uint32_t)k;
+    const uint32_t off = block_excl_scan(nc, wsum, &woff[blockDim.x]);
+    woff[threadIdx.x] = off;
+    __syncthreads();
+    const uint32_t W = woff[blockDim.x];
+    for (uint32_t r0 = 0; r0 < W; r0 += blockDim.x) {
+      const uint32_t w = r0 + threadIdx.x;
+      if (w < W) {
+        uint32_t lo = 0, hi = blockDim.x - 1;  // the last thread whose offset is <= w owns it
+        while (lo < hi) {
+          const uint32_t mid = (lo + hi + 1) >> 1;
+          if (woff[mid] <= w) lo = mid;
+          else hi = mid - 1;
+        }
+        const int ko = (int)kslot[lo];
+        const uint32_t id = P.wcand[(size_t)ko * WALL_CAND_CAP + (w - woff[lo])];
+        const D4 xo = B.xr[ko], vo = B.vm[ko], wo = B.wc[ko];
+        V fc, tc;
+        const bool ok = wall_contact(P, law_of(P, B, ko), P.tri[id], xyz(xo), xyz(vo), xyz(wo), xo.w, vo.w, fc, tc,
+                                     excess);
+        wok[threadIdx.x] = ok ? 1 : 0;
+        if (ok) {
+          wres[0][threadIdx.x] = fc.x; wres[1][threadIdx.x] = fc.y; wres[2][threadIdx.x] = fc.z;
+          wres[3][threadIdx.x] = tc.x; wres[4][threadIdx.x] = tc.y; wres[5][threadIdx.x] = tc.z;
+        }
+      }
+      __syncthreads();
+      const uint32_t a = max(off, r0), b = min(off + nc, r0 + blockDim.x);
+      for (uint32_t q = a; q < b; ++q) {
+        const uint32_t sl = q - r0;
+        if (wok[sl]) {
+          F = F + vmk(wres[0][sl], wres[1][sl], wres[2][sl]);
+          T = T + vmk(wres[3][sl], wres[4][sl], wres[5][sl]);
+        }
+      }
+      __syncthreads();
+    }
+    if (!live) continue;
+    if (qe.y > WALL_CAND_CAP) {  // candidates past the cap, inline, still in mesh order
+      const float4 xf = B.xf[k];
+      uint32_t s = 0, e = 0;
+      tri_cell_range(P, xf, s, e);
+      const float xmag = fmaxf(fmaxf(fabsf(xf.x), fabsf(xf.y)), fabsf(xf.z));
+      const uint32_t gi = P.ngroups > 1 ? B.grp[k] : 0u;
       const D4 xi4 = B.xr[k], vi4 = B.vm[k], wi4 = B.wc[k];
-      wall_forces(P, law_of(P, B, k), P.ngroups > 1 ? B.grp[k] : 0u, xyz(xi4), B.xf[k], xyz(vi4), xyz(wi4), xi4.w,
-                  vi4.w, F, T, excess);
+      const Law L = law_of(P, B, k);
+      uint32_t seen = 0;
+      for (uint32_t t = s; t < e; ++t) {
+        const TriRec& tr = P.tri[P.titems[t]];
+        if (!wall_pretest(tr, gi, xf, xmag)) continue;
+        if (seen++ < WALL_CAND_CAP) continue;  // evaluated in the dense rounds
+        V fc, tc;
+        if (wall_contact(P, L, tr, xyz(xi4), xyz(vi4), xyz(wi4), xi4.w, vi4.w, fc, tc, excess)) {
+          F = F + fc;
+          T = T + tc;
+        }
+      }
     }
-    if (P.debug) {
-      P.dbgF[3 * (size_t)k] = F.x; P.dbgF[3 * (size_t)k + 1] = F.y; P.dbgF[3 * (size_t)k + 2] = F.z;
-      P.dbgT[3 * (size_t)k] = T.x; P.dbgT[3 * (size_t)k + 1] = T.y; P.dbgT[3 * (size_t)k + 2] = T.z;
-    }
-    // non-finite check and the +0 of 0 + T on the integer pipe
-    if (!(finite_bits(F.x) & finite_bits(F.y) & finite_bits(F.z) & finite_bits(T.x) & finite_bits(T.y) &
-          finite_bits(T.z)))
-      atomicOr(&C->status, (unsigned)ST_NAN);
-    const V a = vmk(P.gravity[0], P.gravity[1], P.gravity[2]) + F * B.vres[k].w;  // F (1/m)
-    const V tau = vmk(plus_zero(T.x), plus_zero(T.y), plus_zero(T.z));
-    B.acc[k] = D4{a.x, a.y, a.z, 0.0};
-    B.tq[k] = D4{tau.x, tau.y, tau.z, 0.0};
+    finish_particle(P, B, C, k, F, T);
   }
   if (excess) C->overlap_flag = 1;
 }
@@ -1365,6 +1567,10 @@ static int launch_contact_path(const StepParams& P, cudaStream_t s) {
     ++launched;
   }
   k_accumulate<<<shaped_grid((uint64_t)P.n, ba, cap), ba, 0, s>>>(P);
+  if (P.ntri > 0) {  // over the queue k_accumulate filled; its length is only known on the device
+    k_accumulate_walls<<<shaped_grid((uint64_t)P.n, 128, 152 * 16), 128, 0, s>>>(P);
+    ++launched;
+  }
   return launched;
 }
 

@@ -63,6 +63,7 @@ struct Law {
   float jkr_Cf, pad_;
 };
 constexpr uint32_t GROUP_ALL = 0xFFFFFFFFu;
+constexpr uint32_t WALL_CAND_CAP = 8;  // wall candidates held per particle between the accumulate kernels
 
 // A rigid surface velocity V + W x (p - C) of a set of triangles whose geometry
 // stays put (a surface of revolution turning about its own axis, a belt). The
@@ -127,11 +128,14 @@ struct StepParams {
   // contact-parallel buffers (recomputed every step)
   CRec* crec;       // n*cap records, row k at k*cap
   uint32_t* ccnt;   // records per particle
+  uint32_t* aorder; // slots in the order k_accumulate visits them (a permutation within tiles of 256)
+  uint2* wq;        // (slot, wall candidates) of the particles with a wall candidate; length ctot[4]
+  uint32_t* wcand;  // per slot, the first WALL_CAND_CAP triangles that passed the wall pretest
   uint32_t* ncomp;  // records that evaluate their pair (each pair once)
   uint32_t* coff;   // exclusive scan of ccnt: result offset of particle k
   uint32_t* poff;   // exclusive scan of ncomp
   uint32_t* clist;  // compact list of evaluating record slots
-  uint32_t* ctot;   // [0] records, [1] evaluating records, [2] network queue, [3] deferred pairs
+  uint32_t* ctot;   // [0] records, [1] evaluating records, [2] network queue, [3] deferred pairs, [4] wall queue
   uint32_t* jfb;    // evaluating indices deferred to the reference-Newton pass (null: no deferral)
   double* cres;     // per record: force (3) and torque (3) on the row's particle
   uint32_t* cpart;  // scan partials
@@ -140,6 +144,7 @@ struct StepParams {
   int debug;
   double dt;
   double bmin[3], bmax[3], bsize[3];
+  float bsizef[3];  // (float)bsize: FP32 kernels take no double-to-float conversion per use
   double gravity[3];
   Material pm, wm;
   Law law;             // group 0 (the host's copy; kernels read glaw)

@@ -43,6 +43,7 @@ int launch_second_half(const StepParams& P, cudaStream_t s);
 int launch_rebuild_condition(const StepParams& P, cudaGraphConditionalHandle h, cudaStream_t s);
 int launch_end_step_loop(const StepParams& P, cudaGraphConditionalHandle loop, cudaStream_t s);
 int launch_force(const StepParams& P, cudaStream_t s);
+int launch_accum_order(const StepParams& P, cudaStream_t s);  // inside the rebuild chain, before the bank flip
 int launch_end_step(const StepParams& P, cudaStream_t s);
 // Kinetic energy (translational + rotational) of the live slots, FP64.
 void launch_kinetic_energy(const StepParams& P, double* out, cudaStream_t s);

@@ -153,6 +153,36 @@ def test_one_step_walls(rp, oracle_mod):
         compare_step(o, g)
 
 
+def test_one_step_fine_floor_many_wall_contacts(rp, oracle_mod):
+    # a floor of 1 mm triangles under spheres of radius 4-6 mm pressed 0.3-1 mm
+    # into it: every triangle within a radius of the centre is a contact of
+    # its own (src/simulation.rs:464-523), dozens per sphere, in mesh order
+    lo, hi = (-0.1, -0.05, -0.1), (0.1, 0.1, 0.1)
+    m = 80
+    xs = np.linspace(-0.04, 0.04, m + 1)
+    v = []
+    for i in range(m):
+        for j in range(m):
+            a, b, c, d = (xs[i], 0, xs[j]), (xs[i + 1], 0, xs[j]), (xs[i], 0, xs[j + 1]), (xs[i + 1], 0, xs[j + 1])
+            v += [a + c + b, b + c + d]
+    v = np.array(v, np.float32).astype(np.float64)
+    n = np.tile([0.0, 1.0, 0.0], (len(v), 1))
+    rng = np.random.default_rng(41)
+    g = np.stack(np.meshgrid(np.arange(6), np.arange(12), indexing="ij"), -1).reshape(-1, 2)
+    k = len(g)
+    r = rng.uniform(0.004, 0.006, k)
+    x = np.stack([-0.0325 + g[:, 0] * 0.013, r - rng.uniform(0.0003, 0.001, k), -0.0358 + g[:, 1] * 0.0065], 1)
+    x[g[:, 1] % 2 == 1, 1] += 0.02  # every other row clear of the floor; no sphere touches another
+    st = {"position": x, "radius": r, "mass": 2500.0 * 4.0 / 3.0 * np.pi * r ** 3,
+          "velocity": rng.normal(0, 0.05, (k, 3)), "angular_velocity": rng.normal(0, 1.0, (k, 3)),
+          "acceleration": np.zeros((k, 3)), "torque": np.zeros((k, 3)), "fixed": np.zeros(k, np.uint8)}
+    o, g = one_step(rp, oracle_mod, st, 1, 0, lo, hi, tris=(v, n), cell=0.02,
+                    wall=(1e8, 0.25, 7800.0, 0.3, 0.6, 0.0))
+    compare_step(o, g)
+    Fo, _ = o.last_forces()
+    assert np.count_nonzero(Fo[:, 1] > 0) == k // 2
+
+
 def test_one_step_physical_mindlin(rp, oracle_mod):
     lo, hi = (-0.25, -0.25, -0.25), (0.25, 0.25, 0.25)
     st = pu.random_bed(31, 2000, lo, hi, 0.008, 0.012)
