@@ -479,6 +479,12 @@ int Engine::build_params() {
     P.bmax[k] = bmax[k];
     P.bsize[k] = bmax[k] - bmin[k];
     P.bsizef[k] = (float)P.bsize[k];
+    {
+      const double q = 0.25 * P.bsize[k];
+      uint64_t b;
+      std::memcpy(&b, &q, sizeof(b));
+      P.bq_hi[k] = (uint32_t)(b >> 32) & 0x7FFFFFFFu;
+    }
     P.gravity[k] = gravity[k];
   }
   P.pm = pm;

@@ -50,6 +50,7 @@ __device__ __forceinline__ bool finite_bits(double x) { return (__double2hiint(x
 __device__ __forceinline__ double plus_zero(double x) {
   return (__double_as_longlong(x) << 1) == 0 ? 0.0 : x;
 }
+__device__ __forceinline__ float plus_zero(float x) { return (__float_as_int(x) << 1) == 0 ? 0.0f : x; }
 
 constexpr double kPi = 3.14159265358979323846;
 
@@ -369,6 +370,7 @@ __device__ __forceinline__ bool pair_contact(const StepParams& P, const Law& L, 
   const T3<R> fnv = fmag * n;
   const R fnm = fabs(fmag);
   T3<R> ft;
+  bool ft_zero = false;  // ft is +0: F = fn + 0 without the additions
   if (P.tmodel == 0) {
     if (F32) {
       const T3<R> vt = rv - dot(rv, n) * n;
@@ -377,10 +379,21 @@ __device__ __forceinline__ bool pair_contact(const StepParams& P, const Law& L, 
     }
     ft = coulomb_force<R>(fnm, rv, n, (R)L.mu);
   } else if (!PHYS) {
-    // G* = 0 (src/material.rs:39-50): the spring force is +-0, or NaN when
-    // Mindlin takes sqrt of a negative overlap.
-    R kt = P.tmodel == 2 ? R(8) * (R)L.gs_pp * sqrt(rs * overlap) : (R)L.gs_pp * rs;
-    ft = (kt != kt) ? t3(kt, kt, kt) : t3(R(0), R(0), R(0));
+    // G* = 0 in parity mode (src/material.rs:39-50): the spring force is
+    // 0 * (...), +-0, or NaN when Mindlin's sqrt(R* delta) is NaN or infinite
+    // (a negative overlap); decided without the square root. With +0 for
+    // the spring, F = fn + 0 is fn with -0 made +0.
+    const R y = P.tmodel == 2 ? rs * overlap : rs;
+    const R big = sizeof(R) == sizeof(float) ? R(FLT_MAX) : R(DBL_MAX);
+    const bool finite = P.tmodel == 2 ? (y >= R(0) && y <= big) : (fabs(y) <= big);
+    if (finite) {
+      ft_zero = true;
+      ft = t3(R(0), R(0), R(0));
+    } else {
+      const R nan = sizeof(R) == sizeof(float) ? (R)__int_as_float(0x7fc00000)
+                                               : (R)__longlong_as_double(0x7ff8000000000000ll);
+      ft = t3(nan, nan, nan);
+    }
   } else {
     T3<R> xi_s = t3(R(0), R(0), R(0));
     if (overlap > R(0)) {
@@ -397,7 +410,7 @@ __device__ __forceinline__ bool pair_contact(const StepParams& P, const Law& L, 
       hist[2 * plane] = (double)xi_s.z;
     }
   }
-  const T3<R> fc = fnv + ft;
+  const T3<R> fc = ft_zero ? t3(plus_zero(fnv.x), plus_zero(fnv.y), plus_zero(fnv.z)) : fnv + ft;
   const T3<R> tc = cross(ra, fc);
   fc_out = cvt<double>(fc);
   tc_out = cvt<double>(tc);
@@ -814,10 +827,16 @@ __device__ __forceinline__ bool pretest_far(const StepParams& P, float4 xif, flo
   return d2f > cutf * cutf + band;
 }
 
+// Minimum image on the periodic axes. A difference whose magnitude has a
+// smaller high word than bsize/4 is below bsize/4 (and NaN is not), so it
+// needs no FP64 comparison.
+__device__ __forceinline__ bool near_axis(double d, uint32_t q_hi) {
+  return (uint32_t)(__double2hiint(d) & 0x7FFFFFFF) < q_hi;
+}
 __device__ __forceinline__ V mic(const StepParams& P, V d) {
-  if (P.periodic[0]) { if (d.x > P.bsize[0] * 0.5) d.x = d.x - P.bsize[0]; else if (d.x < -P.bsize[0] * 0.5) d.x = d.x + P.bsize[0]; }
-  if (P.periodic[1]) { if (d.y > P.bsize[1] * 0.5) d.y = d.y - P.bsize[1]; else if (d.y < -P.bsize[1] * 0.5) d.y = d.y + P.bsize[1]; }
-  if (P.periodic[2]) { if (d.z > P.bsize[2] * 0.5) d.z = d.z - P.bsize[2]; else if (d.z < -P.bsize[2] * 0.5) d.z = d.z + P.bsize[2]; }
+  if (P.periodic[0] && !near_axis(d.x, P.bq_hi[0])) { if (d.x > P.bsize[0] * 0.5) d.x = d.x - P.bsize[0]; else if (d.x < -P.bsize[0] * 0.5) d.x = d.x + P.bsize[0]; }
+  if (P.periodic[1] && !near_axis(d.y, P.bq_hi[1])) { if (d.y > P.bsize[1] * 0.5) d.y = d.y - P.bsize[1]; else if (d.y < -P.bsize[1] * 0.5) d.y = d.y + P.bsize[1]; }
+  if (P.periodic[2] && !near_axis(d.z, P.bq_hi[2])) { if (d.z > P.bsize[2] * 0.5) d.z = d.z - P.bsize[2]; else if (d.z < -P.bsize[2] * 0.5) d.z = d.z + P.bsize[2]; }
   return d;
 }
 

@@ -145,6 +145,7 @@ struct StepParams {
   double dt;
   double bmin[3], bmax[3], bsize[3];
   float bsizef[3];  // (float)bsize: FP32 kernels take no double-to-float conversion per use
+  uint32_t bq_hi[3]; // high word of the bits of bsize/4: |d| has a smaller high word => |d| < bsize/4
   double gravity[3];
   Material pm, wm;
   Law law;             // group 0 (the host's copy; kernels read glaw)
