@@ -531,14 +531,15 @@ def measured_peaks():
 def profiled_traffic(workload_name, n):
     """DRAM bytes of one force pass (all its kernels) from the committed ncu
     summary (profiles/force_pass_<workload>.json, captured on a smaller bed of
-    the same workload), scaled to n particles (traffic grows with the units)."""
+    the same workload), scaled to n particles (traffic grows with the units),
+    and the FP64-pipe activity of its kernels from the same captures."""
     p = os.path.join(ROOT, "profiles", f"force_pass_{workload_name}.json")
     try:
         with open(p) as f:
             d = json.load(f)
-        return float(d["dram_bytes_per_pass"]) * n / float(d["particles"])
+        return float(d["dram_bytes_per_pass"]) * n / float(d["particles"]), d.get("fp64_pipe_active_pct")
     except (OSError, KeyError, ValueError):
-        return None
+        return None, None
 
 
 # ------------------------------------------------------------ CPU baseline
@@ -715,9 +716,12 @@ def run_ours(args, log):
     alg_bytes = n_now * B0_FP64 + tri * B_TRIANGLE
     peak, peak_kind = measured_peaks()
     achieved = alg_bytes / (force_ms / 1e3) / 1e9
+    traffic, fp64_pct = profiled_traffic(wl["name"], n_now)
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": profiled_traffic(wl["name"], n_now),
-            "kernel": "force pass (k_contact_filter, scans, k_contact_index, k_contact_force, k_accumulate)",
+            "traffic": traffic,
+            "kernel": ("force pass (k_contact_filter, scans, k_contact_index, k_contact_force, k_accumulate, "
+                       "k_accumulate_walls)"),
+            "fp64_pipe_active_pct": fp64_pct,
             "avg_launch_ms": force_ms,
             "force_share_of_step": force_ms / step_ms_profiled if step_ms_profiled > 0 else None,
             "algorithmic_bytes_per_launch": alg_bytes, "peak_source": peak_kind}
@@ -749,7 +753,9 @@ def run_ours(args, log):
         "roofline": roof, "cpu_baseline": cpu,
         "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d / e2e_steps,
                 "d2h_bytes_per_step": d2h / e2e_steps,
-                "note": "set_state (H2D of the full state) + steps(K) + get_state (D2H), K = steps"},
+                "note": "set_state (H2D of the full state) + steps(K) + get_state (D2H), K = steps",
+                "transfer": ("kernels on the caller's pageable arrays (device reaches host memory through the "
+                             "host page tables)" if s1.get("state_io_direct") else "staged copies")},
         "gpu_launches": int(launches), "clocks": ck,
         "stats": {k: s1[k] for k in ("neighbor_rebuilds", "max_neighbors", "neighbor_capacity", "removed")},
     }

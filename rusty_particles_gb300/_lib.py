@@ -61,6 +61,7 @@ class RpStats(ctypes.Structure):
         ("kernel_launches", ctypes.c_uint64),
         ("force_launches", ctypes.c_uint64),
         ("force_ms", ctypes.c_double),
+        ("state_io_direct", ctypes.c_uint64),
     ]
 
 

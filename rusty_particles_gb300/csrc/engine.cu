@@ -12,6 +12,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 
@@ -164,6 +165,8 @@ void Engine::free_device() {
   dfree(ctot_); dfree(cpart_);
   dfree(tri_d_); dfree(tstart_d_); dfree(titems_d_); dfree(glaw_d_); dfree(motions_d_);
   dfree(mlp_d_); dfree(jq_); dfree(jguess_); dfree(nnet_); dfree(noff_); dfree(jfb_);
+  dfree(io_buf_); dfree(slot_of_); dfree(io_flag_);
+  io_n_ = 0;
   jq_alloc_ = 0;
   jfb_alloc_ = 0;
   dfree(ctrl_);
@@ -211,6 +214,15 @@ int Engine::ensure_gpu() {
   TRY(dalloc(&ctrl_, 1));
   CK(cudaMallocHost((void**)&ctrl_h_, sizeof(Ctrl)));
   TRY(dalloc(&ke_, 1));
+  {
+    // kernels may dereference the caller's pageable arrays when the device
+    // reaches host memory coherently through the host's page tables
+    int pageable = 0, host_tables = 0;
+    CK(cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device_));
+    CK(cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device_));
+    const char* staged = std::getenv("RP_STAGED_STATE_IO");
+    io_direct_ = pageable == 1 && host_tables == 1 && !(staged && staged[0] == '1');
+  }
   gpu_ = true;
   return RP_OK;
 }
@@ -316,6 +328,11 @@ int Engine::set_group_material(uint32_t group, const Material& m) {
 }
 
 size_t Engine::count() {
+  if (!host_valid_ && gpu_ && dev_valid_) {
+    // live slots, without bringing the state to the host
+    if (cudaSetDevice(device_) != cudaSuccess || sync_ctrl() != RP_OK) return 0;
+    return (size_t)n_ - (size_t)ctrl_h_->removed;
+  }
   if (!host_valid_) {
     if (download() != RP_OK) return 0;
   }
@@ -791,8 +808,10 @@ int Engine::upload() {
     // correctly rounded division the step would do)
     a8[7][i] = D4{p.wres[0], p.wres[1], p.wres[2], 1.0 / (0.4 * p.m * p.r * p.r)};
     flags[i] = p.fixed ? PF_FIXED : 0u;
-    tags[i] = p.tag;
+    tags[i] = (uint32_t)i;  // the device tag is the id at upload; the insertion tag stays on the host
   }
+  up_tags_.resize(n);
+  for (size_t i = 0; i < n; ++i) up_tags_[i] = hp_[i].tag;
   Bank& B = bank_[0];
   D4* dst[8] = {B.xr, B.vm, B.wc, B.acc, B.tq, B.xres, B.vres, B.wres};
   if (n > 0) {
@@ -877,7 +896,7 @@ int Engine::download() {
     p.r = a8[0][k].w;
     p.m = a8[1][k].w;
     p.fixed = (flags[k] & PF_FIXED) ? 1 : 0;
-    p.tag = tags[k];
+    p.tag = up_tags_[tags[k]];
     p.group = groups[k];
   }
   host_valid_ = true;
@@ -1127,7 +1146,113 @@ int Engine::set_vec(size_t id, int which, const double in[3]) {
   return RP_OK;
 }
 
+int Engine::ensure_io(size_t n) {
+  if (io_buf_ && io_n_ >= n) return RP_OK;
+  TRY(dalloc(&io_buf_, 26 * n + n / 8 + 1));
+  TRY(dalloc(&slot_of_, n));
+  TRY(dalloc(&io_flag_, 1));
+  io_n_ = n;
+  return RP_OK;
+}
+
+// Staging layout in io_buf_: vector q at q*3n, radius at 24n, mass at 25n,
+// fixed bytes at 26n.
+static StateIO state_io(double* buf, size_t n, double* const vec[8], const void* r, const void* m,
+                        const void* f) {
+  StateIO io{};
+  for (int q = 0; q < 8; ++q) io.v[q] = vec[q] ? buf + (size_t)q * 3 * n : nullptr;
+  io.radius = r ? buf + 24 * n : nullptr;
+  io.mass = m ? buf + 25 * n : nullptr;
+  io.fixed = f ? reinterpret_cast<uint8_t*>(buf + 26 * n) : nullptr;
+  return io;
+}
+
+int Engine::fast_read_state(rp_state* st, bool& done) {
+  done = false;
+  if (!gpu_ || !dev_valid_ || n_ <= 0) return RP_OK;
+  CK(cudaSetDevice(device_));
+  TRY(sync_ctrl());
+  if (ctrl_h_->removed != 0 || ctrl_h_->halt != 0) return RP_OK;
+  const size_t n = (size_t)n_;
+  TRY(ensure_io(n));
+  double* vec[8] = {st->position, st->velocity, st->angular_velocity, st->acceleration,
+                    st->torque, st->position_residual, st->velocity_residual, st->angular_velocity_residual};
+  launch_slot_of(P_, slot_of_, stream_);
+  if (io_direct_) {  // the gather writes the caller's arrays
+    StateIO io{};
+    for (int q = 0; q < 8; ++q) io.v[q] = vec[q];
+    io.radius = st->radius;
+    io.mass = st->mass;
+    io.fixed = st->fixed;
+    launch_state_gather(P_, slot_of_, io, stream_);
+    CK(cudaStreamSynchronize(stream_));
+    CK(cudaGetLastError());
+    st->n_particles = n;
+    done = true;
+    return RP_OK;
+  }
+  const StateIO io = state_io(io_buf_, n, vec, st->radius, st->mass, st->fixed);
+  launch_state_gather(P_, slot_of_, io, stream_);
+  for (int q = 0; q < 8; ++q)
+    if (vec[q]) CK(cudaMemcpyAsync(vec[q], io.v[q], sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, stream_));
+  if (st->radius) CK(cudaMemcpyAsync(st->radius, io.radius, sizeof(double) * n, cudaMemcpyDeviceToHost, stream_));
+  if (st->mass) CK(cudaMemcpyAsync(st->mass, io.mass, sizeof(double) * n, cudaMemcpyDeviceToHost, stream_));
+  if (st->fixed) CK(cudaMemcpyAsync(st->fixed, io.fixed, n, cudaMemcpyDeviceToHost, stream_));
+  CK(cudaStreamSynchronize(stream_));
+  CK(cudaGetLastError());
+  st->n_particles = n;
+  done = true;
+  return RP_OK;
+}
+
+int Engine::fast_write_state(const rp_state* st, bool& done) {
+  done = false;
+  if (!gpu_ || !dev_valid_ || n_ <= 0) return RP_OK;
+  CK(cudaSetDevice(device_));
+  TRY(sync_ctrl());
+  if (ctrl_h_->removed != 0 || ctrl_h_->halt != 0) return RP_OK;
+  const size_t n = (size_t)n_;
+  TRY(ensure_io(n));
+  double* const vec[8] = {st->position, st->velocity, st->angular_velocity, st->acceleration,
+                          st->torque, st->position_residual, st->velocity_residual, st->angular_velocity_residual};
+  StateIO io{};
+  launch_slot_of(P_, slot_of_, stream_);
+  if (io_direct_) {  // the kernels read the caller's arrays
+    for (int q = 0; q < 8; ++q) io.v[q] = vec[q];
+    io.radius = st->radius;
+    io.mass = st->mass;
+    io.fixed = st->fixed;
+  } else {
+    io = state_io(io_buf_, n, vec, st->radius, st->mass, st->fixed);
+    for (int q = 0; q < 8; ++q)
+      if (vec[q]) CK(cudaMemcpyAsync(io.v[q], vec[q], sizeof(double) * 3 * n, cudaMemcpyHostToDevice, stream_));
+    if (st->radius) CK(cudaMemcpyAsync(io.radius, st->radius, sizeof(double) * n, cudaMemcpyHostToDevice, stream_));
+    if (st->mass) CK(cudaMemcpyAsync(io.mass, st->mass, sizeof(double) * n, cudaMemcpyHostToDevice, stream_));
+    if (st->fixed) CK(cudaMemcpyAsync(io.fixed, st->fixed, n, cudaMemcpyHostToDevice, stream_));
+  }
+  if (st->radius || st->mass || st->fixed) {
+    // new radii, masses or fixed flags change per-particle constants: only
+    // values equal to the current ones stay on this path
+    launch_state_same(P_, slot_of_, io, io_flag_, stream_);
+    unsigned differs = 0;
+    CK(cudaMemcpyAsync(&differs, io_flag_, sizeof(unsigned), cudaMemcpyDeviceToHost, stream_));
+    CK(cudaStreamSynchronize(stream_));
+    if (differs) return RP_OK;
+  }
+  launch_state_scatter(P_, slot_of_, io, stream_);
+  CK(cudaStreamSynchronize(stream_));
+  CK(cudaGetLastError());
+  host_valid_ = false;  // the device holds the new state
+  done = true;
+  return RP_OK;
+}
+
 int Engine::read_state(rp_state* st) {
+  {
+    bool done = false;
+    TRY(fast_read_state(st, done));
+    if (done) return RP_OK;
+  }
   if (!host_valid_) TRY(download());
   const size_t n = hp_.size();
   st->n_particles = n;
@@ -1147,6 +1272,11 @@ int Engine::read_state(rp_state* st) {
 }
 
 int Engine::write_state(const rp_state* st) {
+  {
+    bool done = false;
+    TRY(fast_write_state(st, done));
+    if (done) return RP_OK;
+  }
   if (!host_valid_) TRY(download());
   const size_t n = hp_.size();
   const double* vec[8] = {st->position, st->velocity, st->angular_velocity, st->acceleration,
@@ -1178,6 +1308,7 @@ int Engine::stats(rp_stats* s) {
   s->kernel_launches = launches_;
   s->force_launches = force_launches_;
   s->force_ms = force_ms_;
+  s->state_io_direct = io_direct_ ? 1u : 0u;
   if (gpu_ && dev_valid_ && n_ > 0) {
     CK(cudaSetDevice(device_));
     launch_kinetic_energy(P_, ke_, stream_);

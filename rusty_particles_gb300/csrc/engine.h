@@ -87,6 +87,7 @@ class Engine {
 
  private:
   std::vector<HostParticle> hp_;  // id order when host_valid_
+  std::vector<uint32_t> up_tags_;  // insertion tags of the uploaded particles; a slot's device tag indexes it
   bool host_valid_ = true, dev_valid_ = false;
   uint32_t next_tag_ = 0;
   std::vector<float> tri_v_, tri_n_;
@@ -165,6 +166,16 @@ class Engine {
   int ensure_gpu();
   int upload();
   int download();
+  // bulk state in id order straight between the caller's arrays and the slots
+  // (valid device state, no dead slot); `done` is false when it does not apply
+  int fast_read_state(rp_state* st, bool& done);
+  int fast_write_state(const rp_state* st, bool& done);
+  int ensure_io(size_t n);
+  double* io_buf_ = nullptr;   // staging: 8 x 3n vectors, radius, mass, fixed
+  bool io_direct_ = false;     // kernels reach the caller's pageable arrays (host page tables)
+  size_t io_n_ = 0;
+  uint32_t* slot_of_ = nullptr;
+  unsigned* io_flag_ = nullptr;
   int alloc_slots(size_t n);
   int alloc_lists(int cap, bool keep_current);
   int build_params();

@@ -1618,4 +1618,93 @@ void launch_kinetic_energy(const StepParams& P, double* out, cudaStream_t s) {
   k_kinetic<<<grid_for(P.n, 256), 256, 0, s>>>(P, out);
 }
 
+// ------------------------------------------------------- bulk state transfer
+// The arrays of rp_read_state / rp_write_state are in id order; a slot's
+// `tag` is its id (the particle's rank at the last upload), so slot_of[id]
+// is a scatter of the tags. Used while no slot is dead (ids are then exactly
+// 0..n-1). Copies only: no arithmetic touches the values.
+__global__ void k_slot_of(StepParams P, uint32_t* slot_of) {
+  const Bank B = P.bank[P.ctrl->bank];
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < P.n; k += gridDim.x * blockDim.x)
+    slot_of[B.tag[k]] = (uint32_t)k;
+}
+
+__global__ void k_state_gather(StepParams P, const uint32_t* slot_of, StateIO io) {
+  const Bank B = P.bank[P.ctrl->bank];
+  const D4* src[8] = {B.xr, B.vm, B.wc, B.acc, B.tq, B.xres, B.vres, B.wres};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n; i += gridDim.x * blockDim.x) {
+    const uint32_t k = slot_of[i];
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+      if (io.v[q]) {
+        const D4 d = src[q][k];
+        io.v[q][3 * (size_t)i] = d.x;
+        io.v[q][3 * (size_t)i + 1] = d.y;
+        io.v[q][3 * (size_t)i + 2] = d.z;
+      }
+    if (io.radius) io.radius[i] = B.xr[k].w;
+    if (io.mass) io.mass[i] = B.vm[k].w;
+    if (io.fixed) io.fixed[i] = (B.flags[k] & PF_FIXED) ? 1 : 0;
+  }
+}
+
+// Whether the given radii, masses and fixed flags equal the current ones (the
+// per-particle constants derived from them then stay valid).
+__global__ void k_state_same(StepParams P, const uint32_t* slot_of, StateIO io, unsigned* differs) {
+  const Bank B = P.bank[P.ctrl->bank];
+  bool d = false;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n; i += gridDim.x * blockDim.x) {
+    const uint32_t k = slot_of[i];
+    if (io.radius && __double_as_longlong(io.radius[i]) != __double_as_longlong(B.xr[k].w)) d = true;
+    if (io.mass && __double_as_longlong(io.mass[i]) != __double_as_longlong(B.vm[k].w)) d = true;
+    if (io.fixed && (io.fixed[i] != 0) != ((B.flags[k] & PF_FIXED) != 0)) d = true;
+  }
+  if (d) atomicOr(differs, 1u);
+}
+
+// Writes the given vector arrays into the slots (the .w fields, radius, mass,
+// cell code, 1/m and 1/I, are kept) and refreshes the FP32 position mirror.
+__global__ void k_state_scatter(StepParams P, const uint32_t* slot_of, StateIO io) {
+  const Bank B = P.bank[P.ctrl->bank];
+  D4* dst[8] = {B.xr, B.vm, B.wc, B.acc, B.tq, B.xres, B.vres, B.wres};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n; i += gridDim.x * blockDim.x) {
+    const uint32_t k = slot_of[i];
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+      if (io.v[q]) {
+        D4 d = dst[q][k];
+        d.x = io.v[q][3 * (size_t)i];
+        d.y = io.v[q][3 * (size_t)i + 1];
+        d.z = io.v[q][3 * (size_t)i + 2];
+        dst[q][k] = d;
+      }
+    if (io.v[0]) {
+      const D4 x = B.xr[k];
+      B.xf[k] = make_float4((float)x.x, (float)x.y, (float)x.z, (float)x.w);
+    }
+  }
+}
+
+void launch_slot_of(const StepParams& P, uint32_t* slot_of, cudaStream_t s) {
+  if (P.n == 0) return;
+  k_slot_of<<<grid_for(P.n, 256), 256, 0, s>>>(P, slot_of);
+}
+
+void launch_state_gather(const StepParams& P, const uint32_t* slot_of, const StateIO& io, cudaStream_t s) {
+  if (P.n == 0) return;
+  k_state_gather<<<grid_for(P.n, 256), 256, 0, s>>>(P, slot_of, io);
+}
+
+void launch_state_same(const StepParams& P, const uint32_t* slot_of, const StateIO& io, unsigned* differs,
+                       cudaStream_t s) {
+  cudaMemsetAsync(differs, 0, sizeof(unsigned), s);
+  if (P.n == 0) return;
+  k_state_same<<<grid_for(P.n, 256), 256, 0, s>>>(P, slot_of, io, differs);
+}
+
+void launch_state_scatter(const StepParams& P, const uint32_t* slot_of, const StateIO& io, cudaStream_t s) {
+  if (P.n == 0) return;
+  k_state_scatter<<<grid_for(P.n, 256), 256, 0, s>>>(P, slot_of, io);
+}
+
 }  // namespace rp

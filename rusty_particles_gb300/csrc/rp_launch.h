@@ -48,4 +48,20 @@ int launch_end_step(const StepParams& P, cudaStream_t s);
 // Kinetic energy (translational + rotational) of the live slots, FP64.
 void launch_kinetic_energy(const StepParams& P, double* out, cudaStream_t s);
 
+// Bulk state transfer in id order (no dead slot): the eight vector arrays of
+// rp_state in the order position, velocity, angular velocity, acceleration,
+// torque and the three residuals (3 doubles per particle each), radius, mass,
+// fixed; a null pointer skips that array. Pointers are device memory.
+struct StateIO {
+  double* v[8];
+  double* radius;
+  double* mass;
+  uint8_t* fixed;
+};
+void launch_slot_of(const StepParams& P, uint32_t* slot_of, cudaStream_t s);  // id -> slot
+void launch_state_gather(const StepParams& P, const uint32_t* slot_of, const StateIO& io, cudaStream_t s);
+void launch_state_same(const StepParams& P, const uint32_t* slot_of, const StateIO& io, unsigned* differs,
+                       cudaStream_t s);
+void launch_state_scatter(const StepParams& P, const uint32_t* slot_of, const StateIO& io, cudaStream_t s);
+
 }  // namespace rp

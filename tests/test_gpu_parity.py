@@ -350,3 +350,50 @@ def test_list_growth_inside_a_stepping_call(rp):
     assert st_small["steps"] == st_big["steps"] == 10
     np.testing.assert_array_equal(s_small["position"], s_big["position"])
     np.testing.assert_array_equal(s_small["velocity"], s_big["velocity"])
+
+
+@pytest.mark.parametrize("staged", [False, True])
+def test_state_transfer_on_device(rp, oracle_mod, monkeypatch, staged):
+    # get_state / set_state on a valid device state go straight between the
+    # caller's arrays and the slots (id order through the per-slot id): by
+    # kernels on the caller's arrays where the device reaches pageable host
+    # memory, else through staged copies (forced here by the variable)
+    monkeypatch.setenv("RP_STAGED_STATE_IO", "1" if staged else "0")
+    lo, hi = (-0.25, -0.25, -0.25), (0.25, 0.25, 0.25)
+    st = pu.random_bed(61, 3000, lo, hi, 0.008, 0.012)
+    g = pu.gpu_sim(rp, st, 1e-5, lo, hi, 1, 0)
+    g.steps(3)
+    if staged:
+        assert g.stats()["state_io_direct"] == 0
+    s1 = g.get_state()
+    s1b = g.get_state()
+    for k in s1:
+        np.testing.assert_array_equal(s1[k], s1b[k])
+    # a partial write keeps everything else
+    v = s1["velocity"] * 1.1
+    g.set_state({"velocity": v})
+    s2 = g.get_state()
+    np.testing.assert_array_equal(s2["velocity"], v)
+    for k in ("position", "angular_velocity", "acceleration", "radius", "mass", "position_residual"):
+        np.testing.assert_array_equal(s2[k], s1[k])
+    # a full write with unchanged radii and masses, then one step, against a
+    # fresh upload of the same state stepped once: positions bit-exact (the
+    # first half does not depend on the new forces), velocities to rounding
+    g.set_state(s2)
+    g2 = pu.gpu_sim(rp, {"position": s2["position"], "radius": s2["radius"], "mass": s2["mass"],
+                         "fixed": s2["fixed"], "velocity": s2["velocity"],
+                         "angular_velocity": s2["angular_velocity"], "acceleration": s2["acceleration"],
+                         "torque": s2["torque"]}, 1e-5, lo, hi, 1, 0)
+    g2.set_state({"position_residual": s2["position_residual"], "velocity_residual": s2["velocity_residual"],
+                  "angular_velocity_residual": s2["angular_velocity_residual"]})
+    g.step()
+    g2.step()
+    a, b = g.get_state(), g2.get_state()
+    np.testing.assert_array_equal(a["position"], b["position"])
+    np.testing.assert_allclose(a["velocity"], b["velocity"], rtol=0, atol=1e-12 * np.abs(b["velocity"]).max())
+    # changed masses take the host path and take effect
+    m = s2["mass"] * 2.0
+    g.set_state({"mass": m})
+    np.testing.assert_array_equal(g.get_state()["mass"], m)
+    g.step()
+    assert np.isfinite(g.get_state()["position"]).all()
