@@ -15,6 +15,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <limits>
+#include <thread>
 
 #include "engine.h"
 
@@ -1167,6 +1168,27 @@ static StateIO state_io(double* buf, size_t n, double* const vec[8], const void*
   return io;
 }
 
+// Writes a zero every 4 KB of each range, in parallel, so that the pages
+// exist before the device writes them: a first touch of a host page from the
+// device costs far more than one from the host. Every byte of the ranges is
+// overwritten by the gather that follows.
+static void touch_pages(const std::vector<std::pair<char*, size_t>>& ranges) {
+  size_t total = 0;
+  for (const auto& r : ranges) total += r.second;
+  const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  const unsigned nt = total < ((size_t)8 << 20) ? 1u : hw;
+  auto work = [&](unsigned t) {
+    for (const auto& r : ranges) {
+      const size_t pages = (r.second + 4095) / 4096;
+      for (size_t q = t; q < pages; q += nt) reinterpret_cast<volatile char*>(r.first)[q * 4096] = 0;
+    }
+  };
+  std::vector<std::thread> th;
+  for (unsigned t = 1; t < nt; ++t) th.emplace_back(work, t);
+  work(0);
+  for (auto& x : th) x.join();
+}
+
 int Engine::fast_read_state(rp_state* st, bool& done) {
   done = false;
   if (!gpu_ || !dev_valid_ || n_ <= 0) return RP_OK;
@@ -1179,6 +1201,13 @@ int Engine::fast_read_state(rp_state* st, bool& done) {
                     st->torque, st->position_residual, st->velocity_residual, st->angular_velocity_residual};
   launch_slot_of(P_, slot_of_, stream_);
   if (io_direct_) {  // the gather writes the caller's arrays
+    std::vector<std::pair<char*, size_t>> ranges;
+    for (int q = 0; q < 8; ++q)
+      if (vec[q]) ranges.emplace_back(reinterpret_cast<char*>(vec[q]), sizeof(double) * 3 * n);
+    if (st->radius) ranges.emplace_back(reinterpret_cast<char*>(st->radius), sizeof(double) * n);
+    if (st->mass) ranges.emplace_back(reinterpret_cast<char*>(st->mass), sizeof(double) * n);
+    if (st->fixed) ranges.emplace_back(reinterpret_cast<char*>(st->fixed), n);
+    touch_pages(ranges);
     StateIO io{};
     for (int q = 0; q < 8; ++q) io.v[q] = vec[q];
     io.radius = st->radius;
