@@ -739,19 +739,23 @@ def run_ours(args, log):
             "avg_launch_ms": force_ms,
             "force_share_of_step": force_ms / step_ms_profiled if step_ms_profiled > 0 else None,
             "algorithmic_bytes_per_launch": alg_bytes, "peak_source": peak_kind}
-    # end to end through the public API with host buffers
+    # end to end through the public API with host buffers: the inputs and the
+    # result arrays are allocated (and their pages populated) before timing
     st = sim.get_state()
+    out_buf = {k: np.empty_like(v) for k, v in st.items()}
+    for v in out_buf.values():
+        v.fill(0)
     e2e_steps = args.steps
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     sim.set_state(st)
     sim.steps(e2e_steps)
-    out = sim.get_state()
+    sim.get_state(out=out_buf)
     wall_e2e = time.perf_counter() - t0
-    h2d = n * (8 * 32 + 4 + 4 + 16)
-    d2h = n * (8 * 32 + 4 + 4)
+    h2d = sum(int(v.nbytes) for v in st.values())  # the arrays handed to set_state
+    d2h = sum(int(v.nbytes) for v in out_buf.values())  # the arrays get_state fills
     e2e_val = allreduce_sum(dist, n * e2e_steps) / allreduce_max(dist, wall_e2e)
-    del out
+    del out_buf
     if rank != 0:
         barrier(dist)
         return 0
@@ -767,9 +771,11 @@ def run_ours(args, log):
         "roofline": roof, "cpu_baseline": cpu,
         "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d / e2e_steps,
                 "d2h_bytes_per_step": d2h / e2e_steps,
-                "note": "set_state (H2D of the full state) + steps(K) + get_state (D2H), K = steps",
-                "transfer": ("kernels on the caller's pageable arrays (device reaches host memory through the "
-                             "host page tables)" if s1.get("state_io_direct") else "staged copies")},
+                "note": ("set_state (H2D of the full state) + steps(K) + get_state(out=...) (D2H into host "
+                         "arrays allocated before timing), K = steps"),
+                "transfer": ("set_state by kernels on the caller's pageable arrays (device reaches host memory "
+                             "through the host page tables); get_state by copies" if s1.get("state_io_direct")
+                             else "staged copies")},
         "gpu_launches": int(launches), "clocks": ck,
         "stats": {k: s1[k] for k in ("neighbor_rebuilds", "max_neighbors", "neighbor_capacity", "removed")},
     }

@@ -249,15 +249,31 @@ class Simulation:
         check(self._L.rp_get_stats(self._h, ctypes.byref(s)))
         return {k: getattr(s, k) for k, _ in RpStats._fields_}
 
-    def get_state(self):
-        """All per-particle state as numpy arrays in id order."""
+    def get_state(self, out=None):
+        """All per-particle state as numpy arrays in id order. `out` (a dict as
+        returned here, e.g. from an earlier call) is filled in place instead of
+        allocating: its arrays must be C-contiguous float64 (uint8 for
+        `fixed`) of the current particle count; keys it lacks are skipped."""
         n = self.get_particle_count()
-        arrs = {k: np.zeros((n, 3)) for k in ("position", "velocity", "angular_velocity", "acceleration", "torque",
-                                              "position_residual", "velocity_residual",
-                                              "angular_velocity_residual")}
-        arrs["radius"] = np.zeros(n)
-        arrs["mass"] = np.zeros(n)
-        arrs["fixed"] = np.zeros(n, np.uint8)
+        if out is not None:
+            shapes = {"radius": (n,), "mass": (n,), "fixed": (n,)}
+            known = {f for f, _ in RpState._fields_} - {"n_particles"}
+            for k, a in out.items():
+                if k not in known:
+                    raise KeyError(f"unknown state array {k!r}")
+                want = np.uint8 if k == "fixed" else np.float64
+                if (not isinstance(a, np.ndarray) or a.dtype != want or not a.flags.c_contiguous
+                        or a.shape != shapes.get(k, (n, 3)) or not a.flags.writeable):
+                    raise ValueError(f"out[{k!r}] must be a writable C-contiguous {np.dtype(want).name} array "
+                                     f"of shape {shapes.get(k, (n, 3))}")
+            arrs = out
+        else:
+            arrs = {k: np.zeros((n, 3)) for k in ("position", "velocity", "angular_velocity", "acceleration",
+                                                  "torque", "position_residual", "velocity_residual",
+                                                  "angular_velocity_residual")}
+            arrs["radius"] = np.zeros(n)
+            arrs["mass"] = np.zeros(n)
+            arrs["fixed"] = np.zeros(n, np.uint8)
         st = RpState()
         st.n_particles = n
         for k, a in arrs.items():

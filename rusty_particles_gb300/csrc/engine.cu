@@ -223,6 +223,10 @@ int Engine::ensure_gpu() {
     CK(cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device_));
     const char* staged = std::getenv("RP_STAGED_STATE_IO");
     io_direct_ = pageable == 1 && host_tables == 1 && !(staged && staged[0] == '1');
+    // reads: copies into resident pageable pages ran at ~150 GB/s on GB300
+    // against ~40 GB/s for the gather writing them from the device
+    const char* rd = std::getenv("RP_DIRECT_STATE_READ");
+    read_direct_ = rd && rd[0] == '1';
   }
   gpu_ = true;
   return RP_OK;
@@ -1200,7 +1204,7 @@ int Engine::fast_read_state(rp_state* st, bool& done) {
   double* vec[8] = {st->position, st->velocity, st->angular_velocity, st->acceleration,
                     st->torque, st->position_residual, st->velocity_residual, st->angular_velocity_residual};
   launch_slot_of(P_, slot_of_, stream_);
-  if (io_direct_) {  // the gather writes the caller's arrays
+  if (io_direct_ && read_direct_) {  // the gather writes the caller's arrays
     std::vector<std::pair<char*, size_t>> ranges;
     for (int q = 0; q < 8; ++q)
       if (vec[q]) ranges.emplace_back(reinterpret_cast<char*>(vec[q]), sizeof(double) * 3 * n);

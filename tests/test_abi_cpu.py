@@ -133,3 +133,26 @@ def test_no_gpu_fails_loudly():
         sim.step()
     with pytest.raises(RuntimeError):
         sim.run(0.01)
+
+
+def test_get_state_into_caller_arrays():
+    sim = rp.Simulation.create(0.001, -1.0, -1.0, -1.0, 1.0, 1.0, 1.0, 10)
+    sim.add_particle(0.1, 0.2, 0.3, 0.05, 1.0)
+    sim.add_particle(-0.1, 0.0, 0.0, 0.07, 2.0, fixed=True)
+    fresh = sim.get_state()
+    out = {k: np.full_like(v, 7) for k, v in fresh.items()}
+    got = sim.get_state(out=out)
+    assert got is out
+    for k in fresh:
+        np.testing.assert_array_equal(out[k], fresh[k])
+    part = {"position": np.zeros((2, 3))}
+    sim.get_state(out=part)
+    np.testing.assert_array_equal(part["position"], fresh["position"])
+    with pytest.raises(ValueError):
+        sim.get_state(out={"position": np.zeros((3, 3))})
+    with pytest.raises(ValueError):
+        sim.get_state(out={"radius": np.zeros(2, np.float32)})
+    with pytest.raises(ValueError):
+        sim.get_state(out={"position": np.zeros((3, 2)).T})
+    with pytest.raises(KeyError):
+        sim.get_state(out={"speed": np.zeros((2, 3))})

@@ -352,13 +352,16 @@ def test_list_growth_inside_a_stepping_call(rp):
     np.testing.assert_array_equal(s_small["velocity"], s_big["velocity"])
 
 
-@pytest.mark.parametrize("staged", [False, True])
-def test_state_transfer_on_device(rp, oracle_mod, monkeypatch, staged):
+@pytest.mark.parametrize("mode", ["default", "staged", "direct_read"])
+def test_state_transfer_on_device(rp, oracle_mod, monkeypatch, mode):
     # get_state / set_state on a valid device state go straight between the
-    # caller's arrays and the slots (id order through the per-slot id): by
-    # kernels on the caller's arrays where the device reaches pageable host
-    # memory, else through staged copies (forced here by the variable)
+    # caller's arrays and the slots (id order through the per-slot id): writes
+    # by kernels on the caller's arrays where the device reaches pageable host
+    # memory, reads by copies; the variables force the staged copies for both
+    # or the gather kernel for reads
+    staged = mode == "staged"
     monkeypatch.setenv("RP_STAGED_STATE_IO", "1" if staged else "0")
+    monkeypatch.setenv("RP_DIRECT_STATE_READ", "1" if mode == "direct_read" else "0")
     lo, hi = (-0.25, -0.25, -0.25), (0.25, 0.25, 0.25)
     st = pu.random_bed(61, 3000, lo, hi, 0.008, 0.012)
     g = pu.gpu_sim(rp, st, 1e-5, lo, hi, 1, 0)
@@ -367,8 +370,11 @@ def test_state_transfer_on_device(rp, oracle_mod, monkeypatch, staged):
         assert g.stats()["state_io_direct"] == 0
     s1 = g.get_state()
     s1b = g.get_state()
+    buf = {k: np.empty_like(v) for k, v in s1.items()}
+    g.get_state(out=buf)
     for k in s1:
         np.testing.assert_array_equal(s1[k], s1b[k])
+        np.testing.assert_array_equal(s1[k], buf[k])
     # a partial write keeps everything else
     v = s1["velocity"] * 1.1
     g.set_state({"velocity": v})
