@@ -952,54 +952,35 @@ __global__ void __launch_bounds__(256) k_contact_filter(StepParams P) {
       const uint32_t cnt = B.ncnt[k];
       const uint32_t* row = B.nbr + (size_t)k * P.cap;
       CRec* out = P.crec + (size_t)k * P.cap;
-      // The row in chunks of 32: the FP32 pretests first, into a mask, then
-      // the visit counts and records for the set bits in row order, so the
-      // integer work runs on the lanes that have candidates left instead of
-      // wherever one lane's pretest passed.
-      for (uint32_t m0 = 0; m0 < cnt; m0 += 32) {
-        const uint32_t mend = min(cnt, m0 + 32u);
-        uint32_t pass = 0;
-        for (uint32_t m = m0; m < mend; ++m) {
-          const float4 xjf = B.xf[row[m]];
-          if (!(P.pretest && pretest_far(P, xif, Xi, xjf, adh)) && !(zdrop && jkr_far_zero(P, lw.jkr_Cf, xif, Xi, xjf)) &&
-              !(sdrop && sjkr_far_zero(P, lw, xif, Xi, xjf))) {
-            pass |= 1u << (m - m0);
+      for (uint32_t m = 0; m < cnt; ++m) {
+        const uint32_t j = row[m];
+        const size_t hi = (size_t)k * P.cap + m;
+        int vij = 0, vji = 0;
+        const float4 xjf = B.xf[j];
+        if (!(P.pretest && pretest_far(P, xif, Xi, xjf, adh)) && !(zdrop && jkr_far_zero(P, lw.jkr_Cf, xif, Xi, xjf)) &&
+            !(sdrop && sjkr_far_zero(P, lw, xif, Xi, xjf))) {
+          if (PHYS) {
+            vij = vji = 1;
           } else {
-            const size_t hi = (size_t)k * P.cap + m;
-            if (HIST) {
-              B.hist[hi] = 0.0;
-              B.hist[plane + hi] = 0.0;
-              B.hist[2 * plane + hi] = 0.0;
-            }
-            if (P.debug) P.dbgMult[hi] = 0;
-          }
-        }
-        while (pass) {
-          const uint32_t m = m0 + (uint32_t)(__ffs(pass) - 1);
-          pass &= pass - 1u;
-          const uint32_t j = row[m];
-          const size_t hi = (size_t)k * P.cap + m;
-          int vij = 1, vji = 1;
-          if (!PHYS) {
             const unsigned long long cj = (unsigned long long)__double_as_longlong(B.wc[j].w);
             vij = ref_visits(P, ci, cj);
             vji = ref_visits(P, cj, ci);
           }
-          if (vij > 0) {
-            const bool evaluates = !(vji > 0 && (uint32_t)k > j);
-            const uint32_t net = (learn && evaluates && jkr_net_hint(P, lw.jkr_Cf, xif, B.xf[j])) ? CREC_NET : 0u;
-            out[nrec] = CRec{j, m | ((uint32_t)vij << 16) | ((uint32_t)vji << 24) | net};
-            ++nrec;
-            if (evaluates) ++ncmp;
-            if (net) ++nnet;
-          } else {
-            if (HIST) {
-              B.hist[hi] = 0.0;
-              B.hist[plane + hi] = 0.0;
-              B.hist[2 * plane + hi] = 0.0;
-            }
-            if (P.debug) P.dbgMult[hi] = 0;
+        }
+        if (vij > 0) {
+          const bool evaluates = !(vji > 0 && (uint32_t)k > j);
+          const uint32_t net = (learn && evaluates && jkr_net_hint(P, lw.jkr_Cf, xif, xjf)) ? CREC_NET : 0u;
+          out[nrec] = CRec{j, m | ((uint32_t)vij << 16) | ((uint32_t)vji << 24) | net};
+          ++nrec;
+          if (evaluates) ++ncmp;
+          if (net) ++nnet;
+        } else {
+          if (HIST) {
+            B.hist[hi] = 0.0;
+            B.hist[plane + hi] = 0.0;
+            B.hist[2 * plane + hi] = 0.0;
           }
+          if (P.debug) P.dbgMult[hi] = 0;
         }
       }
     }
