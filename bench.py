@@ -746,12 +746,14 @@ def run_ours(args, log):
     for v in out_buf.values():
         v.fill(0)
     e2e_steps = args.steps
+    e0 = sim.stats()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     sim.set_state(st)
     sim.steps(e2e_steps)
     sim.get_state(out=out_buf)
     wall_e2e = time.perf_counter() - t0
+    e2e_device_ms = sim.stats()["device_ms"] - e0["device_ms"]  # the steps(K) call alone
     h2d = sum(int(v.nbytes) for v in st.values())  # the arrays handed to set_state
     d2h = sum(int(v.nbytes) for v in out_buf.values())  # the arrays get_state fills
     e2e_val = allreduce_sum(dist, n * e2e_steps) / allreduce_max(dist, wall_e2e)
@@ -772,7 +774,8 @@ def run_ours(args, log):
         "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d / e2e_steps,
                 "d2h_bytes_per_step": d2h / e2e_steps,
                 "note": ("set_state (H2D of the full state) + steps(K) + get_state(out=...) (D2H into host "
-                         "arrays allocated before timing), K = steps"),
+                         "arrays allocated before timing), K = steps, run after the timed steps"),
+                "device_ms_of_steps": e2e_device_ms, "wall_ms": wall_e2e * 1e3,
                 "transfer": ("set_state by kernels on the caller's pageable arrays (device reaches host memory "
                              "through the host page tables); get_state by copies" if s1.get("state_io_direct")
                              else "staged copies")},
