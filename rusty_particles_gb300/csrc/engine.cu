@@ -166,7 +166,8 @@ void Engine::free_device() {
   dfree(ctot_); dfree(cpart_);
   dfree(tri_d_); dfree(tstart_d_); dfree(titems_d_); dfree(glaw_d_); dfree(motions_d_);
   dfree(mlp_d_); dfree(jq_); dfree(jguess_); dfree(nnet_); dfree(noff_); dfree(jfb_);
-  dfree(io_buf_); dfree(slot_of_); dfree(io_flag_);
+  dfree(io_buf_); dfree(slot_of_); dfree(io_flag_); dfree(id_live_); dfree(id_pos_); dfree(slot_of_id_);
+  dfree(id_part_);
   io_n_ = 0;
   jq_alloc_ = 0;
   jfb_alloc_ = 0;
@@ -1155,6 +1156,10 @@ int Engine::ensure_io(size_t n) {
   if (io_buf_ && io_n_ >= n) return RP_OK;
   TRY(dalloc(&io_buf_, 26 * n + n / 8 + 1));
   TRY(dalloc(&slot_of_, n));
+  TRY(dalloc(&id_live_, n));
+  TRY(dalloc(&id_pos_, n));
+  TRY(dalloc(&slot_of_id_, n));
+  TRY(dalloc(&id_part_, scan_parts_needed((uint32_t)n) + 16));
   TRY(dalloc(&io_flag_, 1));
   io_n_ = n;
   return RP_OK;
@@ -1198,12 +1203,12 @@ int Engine::fast_read_state(rp_state* st, bool& done) {
   if (!gpu_ || !dev_valid_ || n_ <= 0) return RP_OK;
   CK(cudaSetDevice(device_));
   TRY(sync_ctrl());
-  if (ctrl_h_->removed != 0 || ctrl_h_->halt != 0) return RP_OK;
-  const size_t n = (size_t)n_;
-  TRY(ensure_io(n));
+  if (ctrl_h_->halt != 0) return RP_OK;
+  const size_t n = (size_t)n_ - (size_t)ctrl_h_->removed;  // ids of the live particles
+  TRY(ensure_io((size_t)n_));
   double* vec[8] = {st->position, st->velocity, st->angular_velocity, st->acceleration,
                     st->torque, st->position_residual, st->velocity_residual, st->angular_velocity_residual};
-  launch_slot_of(P_, slot_of_, stream_);
+  const uint32_t* ids = launch_slot_of(P_, IdMap{slot_of_, id_live_, id_pos_, slot_of_id_, id_part_}, (int)n, stream_);
   if (io_direct_ && read_direct_) {  // the gather writes the caller's arrays
     std::vector<std::pair<char*, size_t>> ranges;
     for (int q = 0; q < 8; ++q)
@@ -1217,7 +1222,7 @@ int Engine::fast_read_state(rp_state* st, bool& done) {
     io.radius = st->radius;
     io.mass = st->mass;
     io.fixed = st->fixed;
-    launch_state_gather(P_, slot_of_, io, stream_);
+    launch_state_gather(P_, ids, io, (int)n, stream_);
     CK(cudaStreamSynchronize(stream_));
     CK(cudaGetLastError());
     st->n_particles = n;
@@ -1225,7 +1230,7 @@ int Engine::fast_read_state(rp_state* st, bool& done) {
     return RP_OK;
   }
   const StateIO io = state_io(io_buf_, n, vec, st->radius, st->mass, st->fixed);
-  launch_state_gather(P_, slot_of_, io, stream_);
+  launch_state_gather(P_, ids, io, (int)n, stream_);
   for (int q = 0; q < 8; ++q)
     if (vec[q]) CK(cudaMemcpyAsync(vec[q], io.v[q], sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, stream_));
   if (st->radius) CK(cudaMemcpyAsync(st->radius, io.radius, sizeof(double) * n, cudaMemcpyDeviceToHost, stream_));
@@ -1243,13 +1248,13 @@ int Engine::fast_write_state(const rp_state* st, bool& done) {
   if (!gpu_ || !dev_valid_ || n_ <= 0) return RP_OK;
   CK(cudaSetDevice(device_));
   TRY(sync_ctrl());
-  if (ctrl_h_->removed != 0 || ctrl_h_->halt != 0) return RP_OK;
-  const size_t n = (size_t)n_;
-  TRY(ensure_io(n));
+  if (ctrl_h_->halt != 0) return RP_OK;
+  const size_t n = (size_t)n_ - (size_t)ctrl_h_->removed;  // ids of the live particles
+  TRY(ensure_io((size_t)n_));
   double* const vec[8] = {st->position, st->velocity, st->angular_velocity, st->acceleration,
                           st->torque, st->position_residual, st->velocity_residual, st->angular_velocity_residual};
   StateIO io{};
-  launch_slot_of(P_, slot_of_, stream_);
+  const uint32_t* ids = launch_slot_of(P_, IdMap{slot_of_, id_live_, id_pos_, slot_of_id_, id_part_}, (int)n, stream_);
   if (io_direct_) {  // the kernels read the caller's arrays
     for (int q = 0; q < 8; ++q) io.v[q] = vec[q];
     io.radius = st->radius;
@@ -1266,13 +1271,13 @@ int Engine::fast_write_state(const rp_state* st, bool& done) {
   if (st->radius || st->mass || st->fixed) {
     // new radii, masses or fixed flags change per-particle constants: only
     // values equal to the current ones stay on this path
-    launch_state_same(P_, slot_of_, io, io_flag_, stream_);
+    launch_state_same(P_, ids, io, io_flag_, (int)n, stream_);
     unsigned differs = 0;
     CK(cudaMemcpyAsync(&differs, io_flag_, sizeof(unsigned), cudaMemcpyDeviceToHost, stream_));
     CK(cudaStreamSynchronize(stream_));
     if (differs) return RP_OK;
   }
-  launch_state_scatter(P_, slot_of_, io, stream_);
+  launch_state_scatter(P_, ids, io, (int)n, stream_);
   CK(cudaStreamSynchronize(stream_));
   CK(cudaGetLastError());
   host_valid_ = false;  // the device holds the new state

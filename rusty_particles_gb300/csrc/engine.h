@@ -176,6 +176,7 @@ class Engine {
   bool read_direct_ = false;   // reads by the gather kernel too (else staged copies)
   size_t io_n_ = 0;
   uint32_t* slot_of_ = nullptr;
+  uint32_t *id_live_ = nullptr, *id_pos_ = nullptr, *slot_of_id_ = nullptr, *id_part_ = nullptr;
   unsigned* io_flag_ = nullptr;
   int alloc_slots(size_t n);
   int alloc_lists(int cap, bool keep_current);

@@ -1623,16 +1623,27 @@ void launch_kinetic_energy(const StepParams& P, double* out, cudaStream_t s) {
 // `tag` is its id (the particle's rank at the last upload), so slot_of[id]
 // is a scatter of the tags. Used while no slot is dead (ids are then exactly
 // 0..n-1). Copies only: no arithmetic touches the values.
-__global__ void k_slot_of(StepParams P, uint32_t* slot_of) {
+__global__ void k_slot_of(StepParams P, uint32_t* slot_of, uint32_t* live) {
   const Bank B = P.bank[P.ctrl->bank];
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < P.n; k += gridDim.x * blockDim.x)
-    slot_of[B.tag[k]] = (uint32_t)k;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < P.n; k += gridDim.x * blockDim.x) {
+    const uint32_t t = B.tag[k];
+    slot_of[t] = (uint32_t)k;
+    live[t] = (B.flags[k] & PF_DEAD) ? 0u : 1u;
+  }
 }
 
-__global__ void k_state_gather(StepParams P, const uint32_t* slot_of, StateIO io) {
+// With removed particles the ids are the live particles in upload order:
+// id = the exclusive scan of the live flags at the upload position.
+__global__ void k_compact_ids(int n, const uint32_t* slot_of, const uint32_t* live, const uint32_t* pos,
+                              uint32_t* slot_of_id) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x)
+    if (live[t]) slot_of_id[pos[t]] = slot_of[t];
+}
+
+__global__ void k_state_gather(StepParams P, const uint32_t* slot_of, StateIO io, int m) {
   const Bank B = P.bank[P.ctrl->bank];
   const D4* src[8] = {B.xr, B.vm, B.wc, B.acc, B.tq, B.xres, B.vres, B.wres};
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n; i += gridDim.x * blockDim.x) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
     const uint32_t k = slot_of[i];
 #pragma unroll
     for (int q = 0; q < 8; ++q)
@@ -1650,10 +1661,10 @@ __global__ void k_state_gather(StepParams P, const uint32_t* slot_of, StateIO io
 
 // Whether the given radii, masses and fixed flags equal the current ones (the
 // per-particle constants derived from them then stay valid).
-__global__ void k_state_same(StepParams P, const uint32_t* slot_of, StateIO io, unsigned* differs) {
+__global__ void k_state_same(StepParams P, const uint32_t* slot_of, StateIO io, unsigned* differs, int m) {
   const Bank B = P.bank[P.ctrl->bank];
   bool d = false;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n; i += gridDim.x * blockDim.x) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
     const uint32_t k = slot_of[i];
     if (io.radius && __double_as_longlong(io.radius[i]) != __double_as_longlong(B.xr[k].w)) d = true;
     if (io.mass && __double_as_longlong(io.mass[i]) != __double_as_longlong(B.vm[k].w)) d = true;
@@ -1664,10 +1675,10 @@ __global__ void k_state_same(StepParams P, const uint32_t* slot_of, StateIO io, 
 
 // Writes the given vector arrays into the slots (the .w fields, radius, mass,
 // cell code, 1/m and 1/I, are kept) and refreshes the FP32 position mirror.
-__global__ void k_state_scatter(StepParams P, const uint32_t* slot_of, StateIO io) {
+__global__ void k_state_scatter(StepParams P, const uint32_t* slot_of, StateIO io, int m) {
   const Bank B = P.bank[P.ctrl->bank];
   D4* dst[8] = {B.xr, B.vm, B.wc, B.acc, B.tq, B.xres, B.vres, B.wres};
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n; i += gridDim.x * blockDim.x) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
     const uint32_t k = slot_of[i];
 #pragma unroll
     for (int q = 0; q < 8; ++q)
@@ -1685,26 +1696,30 @@ __global__ void k_state_scatter(StepParams P, const uint32_t* slot_of, StateIO i
   }
 }
 
-void launch_slot_of(const StepParams& P, uint32_t* slot_of, cudaStream_t s) {
-  if (P.n == 0) return;
-  k_slot_of<<<grid_for(P.n, 256), 256, 0, s>>>(P, slot_of);
+const uint32_t* launch_slot_of(const StepParams& P, const IdMap& M, int live, cudaStream_t s) {
+  if (P.n == 0) return M.slot_of;
+  k_slot_of<<<grid_for(P.n, 256), 256, 0, s>>>(P, M.slot_of, M.live);
+  if (live == P.n) return M.slot_of;  // no removed particle: the ids are the upload positions
+  launch_exclusive_scan(nullptr, M.live, M.pos, (uint32_t)P.n, M.part, nullptr, s);
+  k_compact_ids<<<grid_for(P.n, 256), 256, 0, s>>>(P.n, M.slot_of, M.live, M.pos, M.slot_of_id);
+  return M.slot_of_id;
 }
 
-void launch_state_gather(const StepParams& P, const uint32_t* slot_of, const StateIO& io, cudaStream_t s) {
-  if (P.n == 0) return;
-  k_state_gather<<<grid_for(P.n, 256), 256, 0, s>>>(P, slot_of, io);
+void launch_state_gather(const StepParams& P, const uint32_t* slot_of, const StateIO& io, int m, cudaStream_t s) {
+  if (m == 0) return;
+  k_state_gather<<<grid_for(m, 256), 256, 0, s>>>(P, slot_of, io, m);
 }
 
-void launch_state_same(const StepParams& P, const uint32_t* slot_of, const StateIO& io, unsigned* differs,
+void launch_state_same(const StepParams& P, const uint32_t* slot_of, const StateIO& io, unsigned* differs, int m,
                        cudaStream_t s) {
   cudaMemsetAsync(differs, 0, sizeof(unsigned), s);
-  if (P.n == 0) return;
-  k_state_same<<<grid_for(P.n, 256), 256, 0, s>>>(P, slot_of, io, differs);
+  if (m == 0) return;
+  k_state_same<<<grid_for(m, 256), 256, 0, s>>>(P, slot_of, io, differs, m);
 }
 
-void launch_state_scatter(const StepParams& P, const uint32_t* slot_of, const StateIO& io, cudaStream_t s) {
-  if (P.n == 0) return;
-  k_state_scatter<<<grid_for(P.n, 256), 256, 0, s>>>(P, slot_of, io);
+void launch_state_scatter(const StepParams& P, const uint32_t* slot_of, const StateIO& io, int m, cudaStream_t s) {
+  if (m == 0) return;
+  k_state_scatter<<<grid_for(m, 256), 256, 0, s>>>(P, slot_of, io, m);
 }
 
 }  // namespace rp

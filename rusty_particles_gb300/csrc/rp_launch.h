@@ -48,7 +48,7 @@ int launch_end_step(const StepParams& P, cudaStream_t s);
 // Kinetic energy (translational + rotational) of the live slots, FP64.
 void launch_kinetic_energy(const StepParams& P, double* out, cudaStream_t s);
 
-// Bulk state transfer in id order (no dead slot): the eight vector arrays of
+// Bulk state transfer in id order (ids of the live particles): the eight vector arrays of
 // rp_state in the order position, velocity, angular velocity, acceleration,
 // torque and the three residuals (3 doubles per particle each), radius, mass,
 // fixed; a null pointer skips that array. Pointers are device memory.
@@ -58,10 +58,16 @@ struct StateIO {
   double* mass;
   uint8_t* fixed;
 };
-void launch_slot_of(const StepParams& P, uint32_t* slot_of, cudaStream_t s);  // id -> slot
-void launch_state_gather(const StepParams& P, const uint32_t* slot_of, const StateIO& io, cudaStream_t s);
-void launch_state_same(const StepParams& P, const uint32_t* slot_of, const StateIO& io, unsigned* differs,
+// id -> slot for the `live` particles: slot_of indexed by upload position,
+// then (when some were removed) compacted by a scan of the live flags into
+// slot_of_id. Returns the map to use; buffers of n entries, part for the scan.
+struct IdMap {
+  uint32_t *slot_of, *live, *pos, *slot_of_id, *part;
+};
+const uint32_t* launch_slot_of(const StepParams& P, const IdMap& M, int live, cudaStream_t s);
+void launch_state_gather(const StepParams& P, const uint32_t* slot_of, const StateIO& io, int m, cudaStream_t s);
+void launch_state_same(const StepParams& P, const uint32_t* slot_of, const StateIO& io, unsigned* differs, int m,
                        cudaStream_t s);
-void launch_state_scatter(const StepParams& P, const uint32_t* slot_of, const StateIO& io, cudaStream_t s);
+void launch_state_scatter(const StepParams& P, const uint32_t* slot_of, const StateIO& io, int m, cudaStream_t s);
 
 }  // namespace rp

@@ -403,3 +403,29 @@ def test_state_transfer_on_device(rp, oracle_mod, monkeypatch, mode):
     np.testing.assert_array_equal(g.get_state()["mass"], m)
     g.step()
     assert np.isfinite(g.get_state()["position"]).all()
+
+
+def test_state_transfer_after_removals(rp, oracle_mod):
+    # particles beyond the removal bound are dropped in the first step
+    # (src/simulation.rs:200-219); the bulk transfers then address the live
+    # particles in insertion order, as the per-particle getters (host path) do
+    lo, hi = (-0.25, -0.25, -0.25), (0.25, 0.25, 0.25)
+    st = pu.random_bed(67, 2000, lo, hi, 0.008, 0.012)
+    gone = np.arange(5, 2000, 97)
+    st["position"][gone, 1] = lo[1] - 1.5
+    g = pu.gpu_sim(rp, st, 1e-5, lo, hi, 1, 0)
+    g.steps(2)
+    n = g.get_particle_count()
+    assert n == 2000 - len(gone)
+    s = g.get_state()
+    assert len(s["radius"]) == n
+    keep = np.setdiff1d(np.arange(2000), gone)
+    np.testing.assert_array_equal(s["radius"], st["radius"][keep])
+    v = s["velocity"] * 0.5
+    g.set_state({"velocity": v})
+    s2 = g.get_state()
+    np.testing.assert_array_equal(s2["velocity"], v)
+    np.testing.assert_array_equal(s2["position"], s["position"])
+    for i in (0, 1, n // 2, n - 1):  # per-particle getters read through the host
+        assert g.get_particle_velocity(i) == tuple(v[i])
+        assert g.get_particle_position(i) == tuple(s["position"][i])
