@@ -776,9 +776,8 @@ def run_ours(args, log):
                 "note": ("set_state (H2D of the full state) + steps(K) + get_state(out=...) (D2H into host "
                          "arrays allocated before timing), K = steps, run after the timed steps"),
                 "device_ms_of_steps": e2e_device_ms, "wall_ms": wall_e2e * 1e3,
-                "transfer": ("set_state by kernels on the caller's pageable arrays (device reaches host memory "
-                             "through the host page tables); get_state by copies" if s1.get("state_io_direct")
-                             else "staged copies")},
+                "transfer": ("kernels on the caller's pageable arrays" if s1.get("state_io_direct")
+                             else "one device copy per array, gather/scatter kernels between id order and the slots")},
         "gpu_launches": int(launches), "clocks": ck,
         "stats": {k: s1[k] for k in ("neighbor_rebuilds", "max_neighbors", "neighbor_capacity", "removed")},
     }

@@ -92,10 +92,10 @@ typedef struct rp_stats {
   uint64_t kernel_launches;    /* kernels launched by stepping calls so far */
   uint64_t force_launches;     /* force-kernel launches timed (profiling on) */
   double force_ms;             /* their summed device time (CUDA events on the launching stream) */
-  uint64_t state_io_direct;    /* 1: rp_write_state moves bulk state by kernels that read the
-                                  caller's pageable arrays (the device reaches host memory through the
-                                  host page tables); 0: staged device copies. rp_read_state copies
-                                  into the caller's arrays either way */
+  uint64_t state_io_direct;    /* 1: rp_read_state / rp_write_state move bulk state by kernels on
+                                  the caller's pageable arrays (the device reaches host memory through
+                                  the host page tables; opt-in, RP_DIRECT_STATE_IO=1); 0: staged
+                                  device copies (default) */
 } rp_stats;
 
 #define RP_STATUS_OVERLAP 1u    /* overlap > 20 % of the smaller radius (src/simulation.rs:361-370) */

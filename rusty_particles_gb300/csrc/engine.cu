@@ -222,12 +222,13 @@ int Engine::ensure_gpu() {
     int pageable = 0, host_tables = 0;
     CK(cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device_));
     CK(cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device_));
-    const char* staged = std::getenv("RP_STAGED_STATE_IO");
-    io_direct_ = pageable == 1 && host_tables == 1 && !(staged && staged[0] == '1');
-    // reads: copies into resident pageable pages ran at ~150 GB/s on GB300
-    // against ~40 GB/s for the gather writing them from the device
-    const char* rd = std::getenv("RP_DIRECT_STATE_READ");
-    read_direct_ = rd && rd[0] == '1';
+    // Staged copies by default: into and out of resident pageable pages they
+    // ran at ~150 GB/s on GB300 with a steady time, while kernels on the
+    // caller's arrays took 1-20 ms for the same bytes from run to run (device
+    // walks of the host page tables). RP_DIRECT_STATE_IO=1 selects the kernels.
+    const char* direct = std::getenv("RP_DIRECT_STATE_IO");
+    io_direct_ = pageable == 1 && host_tables == 1 && direct && direct[0] == '1';
+    read_direct_ = io_direct_;
   }
   gpu_ = true;
   return RP_OK;

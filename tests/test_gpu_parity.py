@@ -352,16 +352,14 @@ def test_list_growth_inside_a_stepping_call(rp):
     np.testing.assert_array_equal(s_small["velocity"], s_big["velocity"])
 
 
-@pytest.mark.parametrize("mode", ["default", "staged", "direct_read"])
+@pytest.mark.parametrize("mode", ["staged", "direct"])
 def test_state_transfer_on_device(rp, oracle_mod, monkeypatch, mode):
     # get_state / set_state on a valid device state go straight between the
-    # caller's arrays and the slots (id order through the per-slot id): writes
-    # by kernels on the caller's arrays where the device reaches pageable host
-    # memory, reads by copies; the variables force the staged copies for both
-    # or the gather kernel for reads
+    # caller's arrays and the slots (id order through the per-slot id): by
+    # staged copies, or (opt-in, where the device reaches pageable host memory)
+    # by gather and scatter kernels on the caller's arrays
     staged = mode == "staged"
-    monkeypatch.setenv("RP_STAGED_STATE_IO", "1" if staged else "0")
-    monkeypatch.setenv("RP_DIRECT_STATE_READ", "1" if mode == "direct_read" else "0")
+    monkeypatch.setenv("RP_DIRECT_STATE_IO", "0" if staged else "1")
     lo, hi = (-0.25, -0.25, -0.25), (0.25, 0.25, 0.25)
     st = pu.random_bed(61, 3000, lo, hi, 0.008, 0.012)
     g = pu.gpu_sim(rp, st, 1e-5, lo, hi, 1, 0)
