@@ -228,7 +228,6 @@ int Engine::ensure_gpu() {
     // walks of the host page tables). RP_DIRECT_STATE_IO=1 selects the kernels.
     const char* direct = std::getenv("RP_DIRECT_STATE_IO");
     io_direct_ = pageable == 1 && host_tables == 1 && direct && direct[0] == '1';
-    read_direct_ = io_direct_;
   }
   gpu_ = true;
   return RP_OK;
@@ -1210,7 +1209,7 @@ int Engine::fast_read_state(rp_state* st, bool& done) {
   double* vec[8] = {st->position, st->velocity, st->angular_velocity, st->acceleration,
                     st->torque, st->position_residual, st->velocity_residual, st->angular_velocity_residual};
   const uint32_t* ids = launch_slot_of(P_, IdMap{slot_of_, id_live_, id_pos_, slot_of_id_, id_part_}, (int)n, stream_);
-  if (io_direct_ && read_direct_) {  // the gather writes the caller's arrays
+  if (io_direct_) {  // the gather writes the caller's arrays
     std::vector<std::pair<char*, size_t>> ranges;
     for (int q = 0; q < 8; ++q)
       if (vec[q]) ranges.emplace_back(reinterpret_cast<char*>(vec[q]), sizeof(double) * 3 * n);

@@ -173,7 +173,6 @@ class Engine {
   int ensure_io(size_t n);
   double* io_buf_ = nullptr;   // staging: 8 x 3n vectors, radius, mass, fixed
   bool io_direct_ = false;     // kernels reach the caller's pageable arrays (host page tables)
-  bool read_direct_ = false;   // reads by the gather kernel too (else staged copies)
   size_t io_n_ = 0;
   uint32_t* slot_of_ = nullptr;
   uint32_t *id_live_ = nullptr, *id_pos_ = nullptr, *slot_of_id_ = nullptr, *id_part_ = nullptr;
