@@ -62,7 +62,9 @@ typedef struct rp_sim rp_sim;
 
 /* Host-side state view used by rp_read_state / rp_write_state. Arrays are in
  * particle-id order; vectors hold 3 doubles per particle. Any pointer may be
- * NULL (that field is skipped). rp_write_state ignores n_particles. */
+ * NULL (that field is skipped). n_particles is the length of the caller's
+ * arrays and must equal rp_particle_count(); both calls reject any other value
+ * with RP_E_INVALID_ARG before touching an array. */
 typedef struct rp_state {
   size_t n_particles;
   double* position;         /* 3N */
@@ -240,7 +242,7 @@ typedef struct rp_tune_report {
  * the fastest. The state is not changed. Needs one completed step; not
  * available in physical mode with a spring history. report may be NULL. */
 int rp_autotune(rp_sim* sim, rp_tune_report* report);
-/* Sets the shapes directly (0 = default: 128 threads, 152*64 blocks). */
+/* Sets the shapes directly (0 = default: 128 threads, 64 blocks per multiprocessor). */
 int rp_set_launch_shape(rp_sim* sim, int bs_filter, int bs_force, int bs_accum, int grid_cap);
 
 /* --- learned JKR contact radius (no counterpart in the reference; replaces
@@ -333,7 +335,10 @@ int rp_jkr_samples(const double domain[8], uint64_t seed, size_t n, float* featu
  * The array is shared by every call: calls that overlap on the GPU race and
  * must be serialised by the caller. The first call on a device looks up the
  * array's device address (cudaGetSymbolAddress); make that first call before
- * any stream capture. */
+ * any stream capture. That address is cached for the life of the process and
+ * belongs to the device's current context: after cudaDeviceReset (or any other
+ * teardown of that context) the cache is stale, so do not call this entry
+ * point again in a process that has reset the device. */
 int rp_cell_sort_noalloc(const double* positions, size_t n, const double origin[3], double cell_size,
                          const int32_t dims[3], uint32_t* cell_of, uint32_t* order, void* stream);
 

@@ -286,17 +286,28 @@ class Simulation:
         return arrs
 
     def set_state(self, arrs):
-        """Overwrite per-particle state (keys as in get_state; missing keys are kept)."""
+        """Overwrite per-particle state (keys as in get_state; missing keys are
+        kept). Every array must hold one entry per current particle: shape
+        (n, 3) for vectors and (n,) for radius, mass and fixed, with n =
+        get_particle_count(); ValueError otherwise."""
+        n = self.get_particle_count()
+        known = {f for f, _ in RpState._fields_} - {"n_particles"}
+        for k in arrs:
+            if k not in known:
+                raise KeyError(f"unknown state array {k!r}")
         keep = []
         st = RpState()
+        st.n_particles = n
         for k, _ in RpState._fields_:
             if k == "n_particles" or k not in arrs:
                 continue
+            want = (n,) if k in ("radius", "mass", "fixed") else (n, 3)
+            a = np.ascontiguousarray(arrs[k], np.uint8 if k == "fixed" else np.float64)
+            if a.shape != want:
+                raise ValueError(f"state array {k!r} has shape {a.shape}, expected {want} for {n} particles")
             if k == "fixed":
-                a = np.ascontiguousarray(arrs[k], np.uint8)
                 st.fixed = a.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))
             else:
-                a = np.ascontiguousarray(arrs[k], np.float64)
                 setattr(st, k, _dptr(a))
             keep.append(a)
         check(self._L.rp_write_state(self._h, ctypes.byref(st)))

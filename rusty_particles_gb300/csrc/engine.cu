@@ -599,6 +599,7 @@ int Engine::build_params() {
   P.bs_force = bs_force;
   P.bs_accum = bs_accum;
   P.grid_cap = grid_cap;
+  P.nsm = sm_count();
   P.jkr_solver = jkr_solver;
   for (int k = 0; k < 4; ++k) {
     P.jdom_lo[k] = jkr_dom_[k];
@@ -1539,7 +1540,8 @@ int Engine::autotune(rp_tune_report* rep) {
     ++tried;
     return RP_OK;
   };
-  int cfg[5] = {0, 128, 128, 128, 152 * 64};  // path, filter, pair, accumulate, grid cap
+  const int nsm = P_.nsm;
+  int cfg[5] = {0, 128, 128, 128, nsm * 64};  // path, filter, pair, accumulate, grid cap
   auto apply = [&](const int c[5]) {
     P_.force_path = c[0];
     P_.bs_filter = c[1];
@@ -1552,7 +1554,7 @@ int Engine::autotune(rp_tune_report* rep) {
   TRY(time_pass(&best));
   const float def_ms = best;
   const int blocks[3] = {64, 128, 256};
-  const int caps[3] = {152 * 4, 152 * 16, 152 * 64};
+  const int caps[3] = {nsm * 4, nsm * 16, nsm * 64};
   for (int dim = 1; dim <= 4; ++dim) {
     for (int k = 0; k < 3; ++k) {
       int c[5];

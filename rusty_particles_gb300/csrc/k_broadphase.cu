@@ -7,10 +7,27 @@
 // device control block (rebuild requested and no halt), so a captured step
 // sequence can contain the whole chain and the host never has to sync to
 // decide whether to rebuild.
+#include <atomic>
+
 #include "rp_device.cuh"
 #include "rp_launch.h"
 
 namespace rp {
+
+int sm_count() {
+  static std::atomic<int> cache[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return 1;
+  if (dev >= 64) {
+    int v = 0;
+    return cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && v > 0 ? v : 1;
+  }
+  int v = cache[dev].load(std::memory_order_relaxed);
+  if (v > 0) return v;
+  if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) return 1;
+  cache[dev].store(v, std::memory_order_relaxed);
+  return v;
+}
 
 static constexpr uint32_t EMPTY = 0xFFFFFFFFu;
 static constexpr int RS_BLOCK = 256;

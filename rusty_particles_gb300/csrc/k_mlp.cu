@@ -11,6 +11,7 @@
 #include <cstring>
 #include <vector>
 
+#include "rp_launch.h"
 #include "rp_mlp.cuh"
 
 namespace rp {
@@ -325,7 +326,7 @@ __global__ void __launch_bounds__(128) k_mlp_infer_rows(const MlpInfer* __restri
 
 int grid_of(size_t n, int block) {
   size_t g = (n + block - 1) / block;
-  return (int)std::max<size_t>(1, std::min<size_t>(g, 152 * 32));
+  return (int)std::max<size_t>(1, std::min<size_t>(g, (size_t)sm_count() * 32));
 }
 
 // Round-to-nearest-even FP32 -> BF16 bit pattern (NaN kept quiet).

@@ -37,7 +37,10 @@ static __device__ __align__(256) uint32_t g_noalloc_scratch[NA_WORDS];
 
 // Host-side address of g_noalloc_scratch per device. In host code the symbol
 // name is only a stand-in for the device array; cudaGetSymbolAddress gives the
-// address a kernel can use. Filled once per device by the first call.
+// address a kernel can use. Filled once per device by the first call and kept
+// for the life of the process: it belongs to that device's context, so a
+// process that resets the device (cudaDeviceReset) must not call the entry
+// point again.
 static std::mutex g_noalloc_mu;
 static uint32_t* g_noalloc_ptr[256];
 

@@ -1287,7 +1287,7 @@ __global__ void __launch_bounds__(ACC_TILE) k_accum_order(StepParams P) {
 
 int launch_accum_order(const StepParams& P, cudaStream_t s) {
   const uint64_t tiles = ((uint64_t)P.n + ACC_TILE - 1) / ACC_TILE;
-  k_accum_order<<<(int)std::min<uint64_t>(std::max<uint64_t>(tiles, 1), 152ull * 64ull), ACC_TILE, 0, s>>>(P);
+  k_accum_order<<<(int)std::min<uint64_t>(std::max<uint64_t>(tiles, 1), (uint64_t)P.nsm * 64ull), ACC_TILE, 0, s>>>(P);
   return 1;
 }
 
@@ -1556,7 +1556,7 @@ static int shaped_grid(uint64_t n, int bs, int cap) {
 template <typename R>
 static int launch_contact_path(const StepParams& P, cudaStream_t s) {
   const int bf = P.bs_filter > 0 ? P.bs_filter : 128, bc = P.bs_force > 0 ? P.bs_force : 128,
-            ba = P.bs_accum > 0 ? P.bs_accum : 128, cap = P.grid_cap > 0 ? P.grid_cap : 152 * 64;
+            ba = P.bs_accum > 0 ? P.bs_accum : 128, cap = P.grid_cap > 0 ? P.grid_cap : P.nsm * 64;
   const int g = shaped_grid((uint64_t)P.n, bf, cap);
   const bool hist = P.mode == 1 && P.tmodel != 0;
   if (P.mode == 0) k_contact_filter<false, false><<<g, bf, 0, s>>>(P);
@@ -1572,7 +1572,7 @@ static int launch_contact_path(const StepParams& P, cudaStream_t s) {
   }
   k_contact_index<<<grid_for(P.n, 256), 256, 0, s>>>(P);
   if (learn) {
-    k_jkr_mlp<<<152 * 4, 128, 0, s>>>(P);
+    k_jkr_mlp<<<P.nsm * 4, 128, 0, s>>>(P);
     ++launched;
   }
   const int gc = shaped_grid((uint64_t)P.n * 4, bc, cap);
@@ -1580,14 +1580,14 @@ static int launch_contact_path(const StepParams& P, cudaStream_t s) {
   else if (hist) k_contact_force<true, true, R><<<gc, bc, 0, s>>>(P);
   else k_contact_force<true, false, R><<<gc, bc, 0, s>>>(P);
   if (P.jfb != nullptr) {
-    if (P.mode == 0) k_contact_deferred<false, false, R><<<152 * 8, 128, 0, s>>>(P);
-    else if (hist) k_contact_deferred<true, true, R><<<152 * 8, 128, 0, s>>>(P);
-    else k_contact_deferred<true, false, R><<<152 * 8, 128, 0, s>>>(P);
+    if (P.mode == 0) k_contact_deferred<false, false, R><<<P.nsm * 8, 128, 0, s>>>(P);
+    else if (hist) k_contact_deferred<true, true, R><<<P.nsm * 8, 128, 0, s>>>(P);
+    else k_contact_deferred<true, false, R><<<P.nsm * 8, 128, 0, s>>>(P);
     ++launched;
   }
   k_accumulate<<<shaped_grid((uint64_t)P.n, ba, cap), ba, 0, s>>>(P);
   if (P.ntri > 0) {  // over the queue k_accumulate filled; its length is only known on the device
-    k_accumulate_walls<<<shaped_grid((uint64_t)P.n, 128, 152 * 16), 128, 0, s>>>(P);
+    k_accumulate_walls<<<shaped_grid((uint64_t)P.n, 128, P.nsm * 16), 128, 0, s>>>(P);
     ++launched;
   }
   return launched;

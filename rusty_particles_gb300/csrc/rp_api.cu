@@ -453,10 +453,18 @@ int rp_write_vtk(rp_sim* s, const char* path) {
   return s->e->write_vtk(path);
 }
 
+// Both directions move n_particles entries per array: the caller declares the
+// length of its arrays there, and a length other than the live particle count
+// is rejected before any array is touched.
 int rp_read_state(rp_sim* s, rp_state* out) {
   SIM_OR_FAIL(s);
   if (!out) {
     set_error("null state");
+    return RP_E_INVALID_ARG;
+  }
+  const size_t n = s->e->count();
+  if (out->n_particles != n) {
+    set_error("state arrays hold %zu particles, the simulation has %zu", out->n_particles, n);
     return RP_E_INVALID_ARG;
   }
   return s->e->read_state(out);
@@ -465,6 +473,11 @@ int rp_write_state(rp_sim* s, const rp_state* in) {
   SIM_OR_FAIL(s);
   if (!in) {
     set_error("null state");
+    return RP_E_INVALID_ARG;
+  }
+  const size_t n = s->e->count();
+  if (in->n_particles != n) {
+    set_error("state arrays hold %zu particles, the simulation has %zu", in->n_particles, n);
     return RP_E_INVALID_ARG;
   }
   return s->e->write_state(in);

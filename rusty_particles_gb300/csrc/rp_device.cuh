@@ -125,6 +125,7 @@ struct StepParams {
   // block of the filter, pair and accumulate kernels (<= 256), and the
   // largest grid of their grid-stride loops
   int bs_filter, bs_force, bs_accum, grid_cap;
+  int nsm;  // multiprocessors of the device (sizes the default grids)
   // contact-parallel buffers (recomputed every step)
   CRec* crec;       // n*cap records, row k at k*cap
   uint32_t* ccnt;   // records per particle

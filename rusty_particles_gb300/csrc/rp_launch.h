@@ -8,9 +8,13 @@
 
 namespace rp {
 
+// Multiprocessors of the current CUDA device (cudaDevAttrMultiProcessorCount,
+// looked up once per device; 152 on GB300).
+int sm_count();
+
 inline int grid_for(uint64_t n, int block) {
   uint64_t g = (n + block - 1) / block;
-  const uint64_t cap = 152ull * 64ull;  // 152 SMs; grid-stride loops cover the rest
+  const uint64_t cap = (uint64_t)sm_count() * 64ull;  // grid-stride loops cover the rest
   if (g < 1) g = 1;
   if (g > cap) g = cap;
   return (int)g;

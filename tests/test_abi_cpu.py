@@ -4,6 +4,7 @@ to the reference's exception types; host-only calls (model names, STL
 loading, getters before the first step, VTK output) behave like the
 reference's; stepping without a GPU fails loudly instead of falling back.
 """
+import ctypes
 import os
 import re
 
@@ -156,3 +157,27 @@ def test_get_state_into_caller_arrays():
         sim.get_state(out={"position": np.zeros((3, 2)).T})
     with pytest.raises(KeyError):
         sim.get_state(out={"speed": np.zeros((2, 3))})
+
+
+def test_set_state_checks_lengths():
+    sim = rp.Simulation.create(0.001, -1.0, -1.0, -1.0, 1.0, 1.0, 1.0, 10)
+    sim.add_particle(0.1, 0.2, 0.3, 0.05, 1.0)
+    sim.add_particle(-0.1, 0.0, 0.0, 0.07, 2.0)
+    sim.set_state({"velocity": np.ones((2, 3)), "mass": np.array([1.5, 2.5])})
+    assert sim.get_particle_velocity(1) == (1.0, 1.0, 1.0)
+    assert sim.get_state()["mass"].tolist() == [1.5, 2.5]
+    for bad in ({"velocity": np.ones((1, 3))}, {"position": np.ones(6)}, {"radius": np.ones(3)},
+                {"fixed": np.ones((2, 3), np.uint8)}):
+        with pytest.raises(ValueError):
+            sim.set_state(bad)
+    with pytest.raises(KeyError):
+        sim.set_state({"speed": np.ones((2, 3))})
+    # the C ABI itself rejects a length other than the particle count
+    L = _lib.load()
+    st = _lib.RpState()
+    v = np.ones((3, 3))
+    st.n_particles = 3
+    st.velocity = v.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    assert L.rp_write_state(sim._h, ctypes.byref(st)) == _lib.RP_E_INVALID_ARG
+    assert L.rp_read_state(sim._h, ctypes.byref(st)) == _lib.RP_E_INVALID_ARG
+    assert sim.get_particle_velocity(1) == (1.0, 1.0, 1.0)

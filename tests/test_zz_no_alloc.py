@@ -70,6 +70,33 @@ def test_two_calls_match_allocating_path(env, case):
     assert len(results[0]) != len(results[1])
 
 
+def test_calls_allocate_nothing(env):
+    # After one warm-up call (which looks up the scratch array's address), the
+    # entry point must not change the device's free memory: every buffer is
+    # the caller's, every temporary lives in the static array.
+    torch, rp, L = env
+    n = 100_000
+    rng = np.random.default_rng(5)
+    dpos = torch.from_numpy(rng.uniform(-0.5, 0.5, 3 * n)).cuda()
+    cell = torch.empty(n, dtype=torch.int32, device="cuda")
+    order = torch.empty(n, dtype=torch.int32, device="cuda")
+    origin = (ctypes.c_double * 3)(-0.5, -0.5, -0.5)
+    d = (ctypes.c_int32 * 3)(21, 21, 21)
+    stream = torch.cuda.current_stream().cuda_stream
+    args = (ctypes.cast(dpos.data_ptr(), ctypes.POINTER(ctypes.c_double)), n, origin, 0.05, d,
+            ctypes.c_void_p(cell.data_ptr()), ctypes.c_void_p(order.data_ptr()), ctypes.c_void_p(stream))
+    assert L.rp_cell_sort_noalloc(*args) == 0, L.rp_last_error()
+    torch.cuda.synchronize()
+    first = order.cpu().clone()
+    free_before = torch.cuda.mem_get_info()[0]
+    for _ in range(3):
+        assert L.rp_cell_sort_noalloc(*args) == 0, L.rp_last_error()
+    torch.cuda.synchronize()
+    free_after = torch.cuda.mem_get_info()[0]
+    assert free_before - free_after < (1 << 20), (free_before, free_after)
+    assert torch.equal(order.cpu(), first)
+
+
 def test_rejects_oversized_input(env):
     torch, rp, L = env
     origin = (ctypes.c_double * 3)(0.0, 0.0, 0.0)
