@@ -542,7 +542,20 @@ def profiled_traffic(workload_name, n):
         return None, None
 
 
-# ------------------------------------------------------------ CPU baseline
+# ------------------------------------------------------ CPU side (the oracle)
+STATE_VEC = ("position", "velocity", "angular_velocity", "acceleration", "torque", "position_residual",
+             "velocity_residual", "angular_velocity_residual")
+ORACLE_KEYS = {"position": "x", "velocity": "v", "acceleration": "a", "angular_velocity": "w", "torque": "tau",
+               "position_residual": "xres", "velocity_residual": "vres", "angular_velocity_residual": "wres"}
+
+
+def max_cutoff(wl):
+    """The largest pair cutoff of the workload: 2 r_max, times 1.5 for the
+    adhesive laws (the reference's margin, src/simulation.rs:343-357)."""
+    adh = 1.5 if wl["normal"] in ("jkr", "sjkr") else 1.0
+    return 2.0 * float(np.max(wl["radius"])) * adh
+
+
 def cpu_sample(wl, n_sample, seed=3):
     """A compact sub-block of the bed: the n_sample particles nearest the bed's
     centre of mass, with the workload's full mesh."""
@@ -553,49 +566,463 @@ def cpu_sample(wl, n_sample, seed=3):
     return idx
 
 
-def run_oracle_sample(wl, idx, steps, threads):
+def oracle_for(wl, state=None, prec=64, cell=1.0, cull=False, idx=None, mode=0, material=None, tri_sel=None):
+    """The oracle on the workload (or the particles idx of it), from `state`
+    (arrays as get_state returns them) or from the workload's start."""
     from oracle import oracle as om
     om.build()
-    if threads:
-        om.set_threads(threads)
     lo, hi = wl["lo"], wl["hi"]
-    o = om.OracleSimulation(wl["dt"], lo, hi, prec=64)
-    o.set_mode(0)
+    o = om.OracleSimulation(wl["dt"], lo, hi, prec=prec)
+    o.set_mode(mode)
+    o.set_cell_size(cell)
     o.set_options(record_pairs=False, keep_contact_map=True)
-    o.set_particle_material(*wl["material"])
+    o.set_particle_material(*(material or wl["material"]))
     o.set_contact_models(wl["normal"], wl["tangential"])
     o.set_periodic_boundary(*wl["periodic"])
-    for i in idx:
-        p = wl["position"][i]
-        o.add_particle(p[0], p[1], p[2], wl["radius"][i], wl["mass"][i])
-    if len(wl["tri_v"]):
-        o.add_triangles(wl["tri_v"].astype(np.float64), wl["tri_n"].astype(np.float64))
-    if "velocity" in wl:
-        o.set_state({"v": wl["velocity"][idx]})
-    o.steps(1)  # warm-up (grid, contact map, page faults)
+    src = state if state is not None else {"position": wl["position"], "radius": wl["radius"], "mass": wl["mass"]}
+    sel = slice(None) if idx is None else idx
+    o.add_particles(src["position"][sel], src["radius"][sel], src["mass"][sel])
+    tv, tn = wl["tri_v"], wl["tri_n"]
+    if tri_sel is not None:
+        tv, tn = tv[tri_sel], tn[tri_sel]
+    if len(tv):
+        o.add_triangles(tv.astype(np.float64), tn.astype(np.float64), motion=wl.get("tri_motion"))
+    o.set_wall_cull(cull)
+    if state is not None:
+        o.set_state({ORACLE_KEYS[k]: state[k][sel] for k in STATE_VEC if k in state})
+    elif "velocity" in wl:
+        o.set_state({"v": wl["velocity"][sel]})
+    return o
+
+
+def time_oracle(o, n, budget_s, max_steps=200, min_steps=1):
+    """Steps `o` for about budget_s (after one untimed step); particle-steps/s."""
+    t0 = time.perf_counter()
+    o.steps(1)
+    t1 = time.perf_counter() - t0
+    steps = max(min_steps, min(max_steps, int(budget_s / max(t1, 1e-6))))
     t0 = time.perf_counter()
     o.steps(steps)
     dt = time.perf_counter() - t0
-    return len(idx) * steps / dt, dt, om.get_threads()
+    return n * steps / dt, steps, dt
 
 
-def cpu_baseline(wl, budget_s=20.0, threads=0):
-    """Time the reference algorithm on a bounded sample (about budget_s of CPU work)."""
-    n_sample = min(len(wl["radius"]), 4096)
-    idx = cpu_sample(wl, n_sample)
-    rate1, t1, cores = run_oracle_sample(wl, idx, 1, threads)
-    steps = max(1, min(200, int(budget_s / max(t1, 1e-6))))
-    rate, t, cores = run_oracle_sample(wl, idx, steps, threads)
-    return {
-        "value": rate, "unit": UNIT, "cores": cores, "kind": "port",
-        "sample": (f"{len(idx):,} particles nearest the bed centre with all {len(wl['tri_v']):,} triangles, "
-                   f"{steps} steps ({t:.1f} s); literal reference algorithm (1 m cells, every triangle per "
-                   "particle), FP64, OpenMP over particles; its per-particle cost grows with N"),
-    }
+def compare_forces(Fg, Tg, Fo, To, FS, TS, net_floor=1e-3):
+    """Per-particle force and torque errors of one step against the FP64
+    oracle: max |dF_i| / sum_j |f_ij| (the rounding scale of a reordered sum)
+    and max |dF_i| / |F_i| over the particles whose net force is not a
+    near-cancellation (|F_i| >= net_floor sum_j |f_ij|)."""
+    out = {"particles": int(len(Fo))}
+    fin = np.isfinite(Fo).all(1) & np.isfinite(To).all(1)
+    out["nonfinite_mismatch"] = int(np.count_nonzero(fin != (np.isfinite(Fg).all(1) & np.isfinite(Tg).all(1))))
+    for tag, G, O, S in (("force", Fg, Fo, FS), ("torque", Tg, To, TS)):
+        d = np.linalg.norm(G - O, axis=1)[fin]
+        s = S[fin]
+        net = np.linalg.norm(O, axis=1)[fin]
+        pos = s > 0
+        out[f"{tag}_rel_sum"] = float(np.max(d[pos] / s[pos], initial=0.0))
+        out[f"{tag}_abs_where_zero_scale"] = float(np.max(d[~pos], initial=0.0))
+        sel = pos & (net >= net_floor * s)
+        out[f"{tag}_rel_net"] = float(np.max(d[sel] / net[sel], initial=0.0))
+        out[f"{tag}_net_counted"] = int(np.count_nonzero(sel))
+    out["scales"] = (f"rel_sum: |dF_i| / sum_j |f_ij| (per-contact term magnitudes); rel_net: |dF_i| / |F_i| "
+                     f"where |F_i| >= {net_floor:g} sum_j |f_ij|")
+    return out
+
+
+# ------------------------------------------------------------------- GPU side
+def state_of(sim):
+    return sim.get_state()
+
+
+def wl_at(wl, state):
+    """The workload with its particles at `state` (same radii, masses)."""
+    w = dict(wl)
+    w["position"] = state["position"]
+    w["radius"] = state["radius"]
+    w["mass"] = state["mass"]
+    w.pop("velocity", None)
+    return w
+
+
+def set_dynamic_state(sim, state):
+    sim.set_state({k: state[k] for k in STATE_VEC if k != "position" and k in state})
+
+
+def setup_jkr(sim, jkr):
+    if not jkr:
+        return
+    if jkr["solver"] == "learned":
+        sim.set_jkr_network(*jkr["network"])
+    sim.set_jkr_solver(jkr["solver"])
+
+
+def gpu_one_step_forces(rp, wl, state, mode, precision, jkr, cell):
+    """One GPU step from `state` with debug recording and the reference grid
+    cell `cell`; (F, T) per particle in id order, before division by mass."""
+    g = make_sim(rp, wl_at(wl, state), mode, precision)
+    g.set_reference_cell_size(cell)
+    setup_jkr(g, jkr)
+    set_dynamic_state(g, state)
+    g.set_debug(True)
+    g.step()
+    F, T = g.debug_forces()
+    del g
+    return F, T
+
+
+def force_error(rp, wl, state, mode, precision, jkr, cache, log, threads, keep_oracle=False):
+    """The form's one-step force error against the FP64 oracle on the full
+    benchmark state: both sides step once from the same state with the
+    reference grid's cell at the largest cutoff (the oracle's wall loop culled
+    exactly). Batched workloads compare a sample of boxes, each against its own
+    oracle (one reference Simulation per box)."""
+    from oracle import oracle as om
+    om.build()
+    om.set_threads(threads)
+    hc = max_cutoff(wl)
+    t0 = time.perf_counter()
+    Fg, Tg = gpu_one_step_forces(rp, wl, state, mode, precision, jkr, hc)
+    t_gpu = time.perf_counter() - t0
+    m = 0 if mode == "parity" else 1
+    if "groups" in wl:
+        order = np.argsort(wl["counts"], kind="stable")
+        pick = order[np.linspace(0, len(order) - 1, min(8, len(order))).astype(int)]
+        keys = []
+        Fo_l, To_l, FS_l, TS_l, Fg_l, Tg_l = [], [], [], [], [], []
+        t0 = time.perf_counter()
+        for b in pick:
+            idx = np.flatnonzero(wl["groups"] == b)
+            key = ("box", wl["name"], int(b), m)
+            if key not in cache:
+                o = oracle_for(wl, state, cell=hc, cull=True, idx=idx, mode=m, material=wl["group_material"][b],
+                               tri_sel=wl["tri_group"] == b)
+                o.step()
+                cache[key] = (*o.last_forces(), *o.last_force_scale())
+                del o
+            Fo, To, FS, TS = cache[key]
+            Fo_l.append(Fo); To_l.append(To); FS_l.append(FS); TS_l.append(TS)
+            Fg_l.append(Fg[idx]); Tg_l.append(Tg[idx])
+            keys.append(int(b))
+        t_or = time.perf_counter() - t0
+        res = compare_forces(np.concatenate(Fg_l), np.concatenate(Tg_l), np.concatenate(Fo_l), np.concatenate(To_l),
+                             np.concatenate(FS_l), np.concatenate(TS_l))
+        res["boxes"] = keys
+    else:
+        key = (wl["name"], m)
+        t0 = time.perf_counter()
+        if key not in cache:
+            o = oracle_for(wl, state, cell=hc, cull=True, mode=m)
+            o.step()
+            cache[key] = (*o.last_forces(), *o.last_force_scale())
+            if keep_oracle:
+                cache[key + ("oracle",)] = o  # kept for the CPU baseline timing
+            del o
+        t_or = time.perf_counter() - t0
+        Fo, To, FS, TS = cache[key]
+        res = compare_forces(Fg, Tg, Fo, To, FS, TS)
+    res["method"] = (f"one step from the timed run's final state on both sides, reference-grid cell {hc * 1e3:.4g} mm "
+                     "(the largest cutoff) on both" + (", spring history from zero on both" if mode == "physical"
+                                                       else ""))
+    res["seconds"] = {"gpu": round(t_gpu, 2), "oracle": round(t_or, 2)}
+    log(f"force error {wl['name']} {mode}/{precision}{'/' + jkr['solver'] if jkr else ''}: "
+        f"F {res['force_rel_sum']:.2e} (sum scale) {res['force_rel_net']:.2e} (net)")
+    return res
+
+
+def timed(sim, steps, dist, device):
+    """K steps of the device step loop between barriers and synchronisations,
+    with the clock sampler running; device ms from CUDA events on the
+    engine's stream."""
+    import torch
+    torch.cuda.synchronize()
+    s0 = sim.stats()
+    clocks = ClockSampler(device)
+    barrier(dist)
+    torch.cuda.synchronize()
+    clocks.start()
+    t0 = time.perf_counter()
+    sim.steps(steps)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    barrier(dist)
+    ck = clocks.stop()
+    s1 = sim.stats()
+    return s0, s1, wall, ck
+
+
+def roofline_of(sim, wl, n_now, prof_steps):
+    """The force pass's roofline: the same steps issued from the host with
+    CUDA events around every force launch on the engine's stream."""
+    sim._L.rp_set_profiling(sim._h, 1)
+    p0 = sim.stats()
+    sim.steps(prof_steps)
+    p1 = sim.stats()
+    sim._L.rp_set_profiling(sim._h, 0)
+    force_ms = (p1["force_ms"] - p0["force_ms"]) / max(1, p1["force_launches"] - p0["force_launches"])
+    step_ms = (p1["device_ms"] - p0["device_ms"]) / max(1, p1["steps"] - p0["steps"])
+    tri = len(wl["tri_v"])
+    alg_bytes = n_now * B0_FP64 + tri * B_TRIANGLE
+    peak, peak_kind = measured_peaks()
+    achieved = alg_bytes / (force_ms / 1e3) / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": None,
+            "kernel": ("force pass (k_contact_filter, scans, k_contact_index, k_contact_force, k_accumulate, "
+                       "k_accumulate_walls)"),
+            "avg_launch_ms": force_ms, "force_share_of_step": force_ms / step_ms if step_ms > 0 else None,
+            "algorithmic_bytes_per_launch": alg_bytes, "peak_source": peak_kind}
+
+
+def e2e_of(sim, n, steps, dist):
+    """End to end through the public API with host buffers: set_state of the
+    full state, K steps, get_state into arrays allocated before timing."""
+    import torch
+    st = sim.get_state()
+    out_buf = {k: np.empty_like(v) for k, v in st.items()}
+    for v in out_buf.values():
+        v.fill(0)
+    e0 = sim.stats()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sim.set_state(st)
+    sim.steps(steps)
+    sim.get_state(out=out_buf)
+    wall = time.perf_counter() - t0
+    dev_ms = sim.stats()["device_ms"] - e0["device_ms"]
+    h2d = sum(int(v.nbytes) for v in st.values())
+    d2h = sum(int(v.nbytes) for v in out_buf.values())
+    val = allreduce_sum(dist, n * steps) / allreduce_max(dist, wall)
+    return {"value": val, "unit": UNIT, "h2d_bytes_per_step": h2d / steps, "d2h_bytes_per_step": d2h / steps,
+            "note": ("set_state (H2D of the full state) + steps(K) + get_state(out=...) (D2H into host arrays "
+                     "allocated before timing), K = steps, run after the timed steps"),
+            "device_ms_of_steps": dev_ms, "wall_ms": wall * 1e3,
+            "transfer": ("kernels on the caller's pageable arrays" if sim.stats().get("state_io_direct")
+                         else "one device copy per array, gather/scatter kernels between id order and the slots")}
+
+
+def run_form(rp, wl, args, dist, device, log, *, mode="parity", precision="fp64", jkr=None, state=None, settle=0,
+             steps=None, warmup=None, prof_steps=None, autotune=False, host_loop=False, keep=False):
+    """One form of a workload: build the simulation (from `state` when given),
+    untimed settle and warm-up steps, the timed steps, the force-pass roofline
+    and the end-to-end run. Returns (sim or None, result, final state)."""
+    steps = steps or args.steps
+    warmup = max(3, warmup if warmup is not None else args.warmup)
+    sim = make_sim(rp, wl if state is None else wl_at(wl, state), mode, precision)
+    sim._L.rp_enable_gpu(sim._h, device)
+    if host_loop:
+        sim._L.rp_set_device_loop(sim._h, 0)
+    setup_jkr(sim, jkr)
+    if state is not None:
+        set_dynamic_state(sim, state)
+    if settle:
+        t_settle = time.time()
+        sim.steps(settle)
+        log(f"{wl['name']} {mode}/{precision}: settled {settle} steps in {time.time() - t_settle:.1f} s")
+    sim.steps(warmup)
+    tune = sim.autotune() if autotune else None
+    c0 = sim.jkr_counters() if jkr else None
+    s0, s1, wall, ck = timed(sim, steps, dist, device)
+    dev_ms = s1["device_ms"] - s0["device_ms"]
+    n_now = s1["particles"]
+    t_max = allreduce_max(dist, dev_ms)
+    value = allreduce_sum(dist, n_now * steps) / (t_max / 1e3)
+    res = {"value": value, "unit": UNIT, "ms_per_step": t_max / steps, "steps": steps, "warmup": warmup,
+           "particles": int(n_now), "mode": mode, "precision": precision, "wall_s_timed": wall,
+           "gpu_launches": int(s1["kernel_launches"] - s0["kernel_launches"]), "clocks": ck,
+           "stats": {k: s1[k] for k in ("neighbor_rebuilds", "max_neighbors", "neighbor_capacity", "removed")}}
+    if jkr:
+        c1 = sim.jkr_counters()
+        d = {k: (c1[k] - c0[k]) / steps for k in c1}
+        ev = d["accepted"] + d["zero"] + d["fallback"]
+        res["jkr"] = {"solver": jkr["solver"], "per_step": d}
+        if ev > 0:
+            res["jkr"]["fraction"] = {"converging": d["accepted"] / ev, "certified_zero": d["zero"] / ev,
+                                      "reference_newton": d["fallback"] / ev}
+    if tune:
+        res["autotune"] = tune
+    res["roofline"] = roofline_of(sim, wl, n_now, prof_steps or min(steps, 200))
+    res["e2e"] = e2e_of(sim, len(wl["radius"]), steps, dist)
+    final = sim.get_state()
+    if keep:
+        return sim, res, final
+    del sim
+    return None, res, final
+
+
+def prepared(rp, wl, log):
+    """The workload's relaxed start (radii grown from 0.6x with overlaps
+    removed, on the product engine; not timed)."""
+    if wl["name"].startswith(("hopper", "adhesive", "batched", "drum")):
+        relax(rp, wl, log=log)
+    return wl
+
+
+def jkr_network(rp, wl, state, log):
+    """Train the JKR network once on the GPU for a workload; returns the arrays
+    set_jkr_network takes and the training report."""
+    sim = make_sim(rp, wl_at(wl, state))
+    rep = sim.train_jkr_network(seed=1)
+    net = sim.get_jkr_network()
+    del sim
+    log(f"JKR network trained in {rep['train_ms']:.0f} ms (held-out rms {rep['val_rms']:.2e})")
+    return net, rep
+
+
+def form_entry(res, force_err=None, extra=None):
+    e = {k: res[k] for k in ("value", "ms_per_step", "particles", "mode", "precision", "clocks", "gpu_launches")}
+    e["e2e"] = {"value": res["e2e"]["value"], "wall_ms": res["e2e"]["wall_ms"],
+                "h2d_bytes_per_step": res["e2e"]["h2d_bytes_per_step"],
+                "d2h_bytes_per_step": res["e2e"]["d2h_bytes_per_step"]}
+    e["roofline_frac"] = res["roofline"]["frac"]
+    e["force_ms"] = res["roofline"]["avg_launch_ms"]
+    if "jkr" in res:
+        e["jkr"] = res["jkr"]
+    if "autotune" in res:
+        e["autotune"] = res["autotune"]
+    if force_err is not None:
+        e["force_err"] = force_err
+    if extra:
+        e.update(extra)
+    return e
+
+
+def settled_state(rp, wl, mode, precision, jkr, settle, device, log):
+    """The state after `settle` untimed steps from the workload's relaxed start."""
+    sim = make_sim(rp, wl, mode, precision)
+    sim._L.rp_enable_gpu(sim._h, device)
+    setup_jkr(sim, jkr)
+    t0 = time.time()
+    sim.steps(settle)
+    st = sim.get_state()
+    del sim
+    log(f"{wl['name']}: settled {settle} steps in {time.time() - t0:.1f} s")
+    return st
+
+
+def run_forms(rp, args, dist, device, log, headline_state, hopper_wl, cache, threads, deadline):
+    """Every spec form beside the plain one, each on its own benchmark
+    workload (see the module docstring); each entry carries its own value,
+    e2e, roofline fraction, force error against the FP64 oracle and clocks."""
+    forms = {}
+    K = args.steps
+
+    def budget_ok(name):
+        if time.time() < deadline:
+            return True
+        forms.setdefault("skipped", []).append(f"{name}: time budget of the run used up")
+        return False
+
+    def attempt(name, fn):
+        if not budget_ok(name):
+            return
+        try:
+            fn()
+        except Exception as ex:  # a failing form must not take the headline with it
+            forms.setdefault("errors", {})[name] = f"{type(ex).__name__}: {ex}"
+            log(f"form {name} failed: {ex}")
+
+    sel = set(args.forms.split(",")) if args.forms else {"hopper", "adhesive", "drum", "batched"}
+
+    def hopper_forms():
+        h = forms.setdefault("hopper-1M", {})
+        _, r, st = run_form(rp, hopper_wl, args, dist, device, log, precision="mixed", state=headline_state)
+        h["mixed"] = form_entry(r, force_error(rp, hopper_wl, headline_state, "parity", "mixed", None, cache, log,
+                                               threads))
+        _, r, st = run_form(rp, hopper_wl, args, dist, device, log, mode="physical", state=headline_state, settle=300)
+        h["physical"] = form_entry(r, force_error(rp, hopper_wl, st, "physical", "fp64", None, cache, log, threads),
+                                   {"note": "300 untimed steps from the settled parity state load the springs"})
+
+    def adhesive_forms():
+        wl = prepared(rp, adhesive_workload(n=int(4_194_304 * args.form_scale)), log)
+        a = forms.setdefault("adhesive-4M", {})
+        st = settled_state(rp, wl, "parity", "fp64", {"solver": "certified"}, wl["settle"], device, log)
+        net, rep = jkr_network(rp, wl, st, log)
+        a["training"] = {k: rep[k] for k in ("train_ms", "val_rms", "val_max", "samples", "steps")}
+        for name, prec, solver in (("certified", "fp64", "certified"), ("learned", "fp64", "learned"),
+                                   ("learned_mixed", "mixed", "learned"), ("newton_mixed", "mixed", "newton"),
+                                   ("newton", "fp64", "newton")):
+            if not budget_ok(f"adhesive {name}"):
+                break
+            jk = {"solver": solver, "network": net}
+            _, r, _ = run_form(rp, wl, args, dist, device, log, precision=prec, jkr=jk, state=st,
+                               prof_steps=min(K, 20))
+            a[name] = form_entry(r, force_error(rp, wl, st, "parity", prec, jk, cache, log, threads))
+        a["note"] = "every solver from the same settled state (1,600 steps of the certified solver)"
+
+    def drum_forms():
+        wl = prepared(rp, drum_workload(n=int(16_777_216 * args.form_scale)), log)
+        d = forms.setdefault("drum-16M", {})
+        _, r, st = run_form(rp, wl, args, dist, device, log, settle=wl["settle"])
+        d["fp64"] = form_entry(r, force_error(rp, wl, st, "parity", "fp64", None, cache, log, threads))
+        _, r, _ = run_form(rp, wl, args, dist, device, log, precision="mixed", state=st)
+        d["mixed"] = form_entry(r, force_error(rp, wl, st, "parity", "mixed", None, cache, log, threads))
+        cache.pop((wl["name"], 0), None)
+        cache.pop((wl["name"], 0, "oracle"), None)
+
+    def batched_forms():
+        wl = prepared(rp, batched_workload(n_boxes=max(8, int(args.boxes * args.form_scale))), log)
+        b = forms.setdefault(wl["name"], {})
+        _, r, st = run_form(rp, wl, args, dist, device, log, settle=wl["settle"], autotune=not args.no_autotune)
+        b["device_loop"] = form_entry(r, force_error(rp, wl, st, "parity", "fp64", None, cache, log, threads),
+                                      {"boxes": int(len(wl["counts"]))})
+        b["one_at_a_time"] = one_at_a_time(rp, wl, min(K, 100))
+
+    if "hopper" in sel:
+        attempt("hopper", hopper_forms)
+    if "adhesive" in sel:
+        attempt("adhesive", adhesive_forms)
+    if "drum" in sel:
+        attempt("drum", drum_forms)
+    if "batched" in sel:
+        attempt("batched", batched_forms)
+    return forms
+
+
+def cpu_baselines(wl, state, cache, threads, budget_s, log):
+    """The reference algorithm on the host cores: (1) on the full settled bed
+    with the reference grid's cell at the largest cutoff (the reference's 1 m
+    cell makes the candidate search O(N^2) at this size) and the wall loop
+    culled exactly, (2) literally (1 m cells, every triangle per particle) on
+    the 4,096 particles nearest the bed centre. FP64, OpenMP over particles."""
+    from oracle import oracle as om
+    om.build()
+    om.set_threads(threads)
+    n = len(state["radius"])
+    hc = max_cutoff(wl)
+    o = cache.pop((wl["name"], 0, "oracle"), None)
+    if o is None:
+        o = oracle_for(wl, state, cell=hc, cull=True)
+    rate, k, t = time_oracle(o, n, budget_s * 0.7, max_steps=200)
+    del o
+    full = {"value": rate, "unit": UNIT, "cores": om.get_threads(), "kind": "port",
+            "sample": (f"the full settled bed ({n:,} particles, {len(wl['tri_v']):,} triangles), {k} steps "
+                       f"({t:.1f} s) of the reference algorithm in FP64 with the reference grid's cell at the "
+                       f"largest cutoff ({hc * 1e3:.4g} mm instead of 1 m) and the every-triangle wall loop culled "
+                       "by a triangle grid (same contacts, same order); OpenMP over particles")}
+    idx = cpu_sample(dict(wl, position=state["position"]), min(n, 4096))
+    lit = oracle_for(wl, state, cell=1.0, cull=False, idx=idx)
+    rate2, k2, t2 = time_oracle(lit, len(idx), budget_s * 0.3, max_steps=200)
+    del lit
+    literal = {"value": rate2, "unit": UNIT, "cores": om.get_threads(), "kind": "port",
+               "sample": (f"{len(idx):,} particles nearest the bed centre with all {len(wl['tri_v']):,} triangles, "
+                          f"{k2} steps ({t2:.1f} s); the literal reference algorithm (1 m cells, every triangle per "
+                          "particle), FP64; its per-particle cost grows with N")}
+    log(f"CPU baseline: {rate:.3e} particle-steps/s (full bed), {rate2:.3e} (literal sample)")
+    return full, literal
 
 
 # -------------------------------------------------------------------- arms
+def common_config(wl, ws):
+    n = len(wl["radius"])
+    return {"workload": wl["name"], "describe": wl["describe"], "particles": int(n), "mode": "parity",
+            "parallelism": f"replicas x{ws}",
+            "l2": f"inputs larger than L2 (particle state {n * 312 / 1e6:.0f} MB)"}
+
+
 def run_reference(args, log):
+    """The reference's CPU step on the host cores (the oracle's restatement in
+    f32, the reference's own precision), on the same workload as the GPU arm:
+    every particle, K timed steps after W warm-up steps, all host threads."""
     ws, rank, _ = dist_info()
     dist = init_dist(ws)
     if rank != 0:
@@ -603,28 +1030,28 @@ def run_reference(args, log):
         return 0
     wl = make_workload(args)
     threads = os.cpu_count() or 1
-    rates = []
     from oracle import oracle as om
     om.build()
     om.set_threads(threads)
-    n_sample = min(len(wl["radius"]), 4096)
-    idx = cpu_sample(wl, n_sample)
-    for _ in range(max(1, args.warmup_ref)):
-        run_oracle_sample(wl, idx, 1, threads)
-    t_all = 0.0
-    for _ in range(args.steps_ref):
-        rate, t, cores = run_oracle_sample(wl, idx, 1, threads)
-        rates.append(rate)
-        t_all += t
-    value = len(idx) * len(rates) / t_all
+    hc = max_cutoff(wl)
+    o = oracle_for(wl, prec=32, cell=hc, cull=True)
+    n = len(wl["radius"])
+    o.steps(max(1, args.warmup))
+    t0 = time.perf_counter()
+    o.steps(args.steps)
+    t = time.perf_counter() - t0
+    value = n * args.steps / t
+    sample = (f"every particle of the workload's seeded start state ({n:,} particles, {len(wl['tri_v']):,} "
+              f"triangles), {args.steps} timed steps after {max(1, args.warmup)} warm-up steps; the reference "
+              f"algorithm in f32 with the reference grid's cell at the largest cutoff ({hc * 1e3:.4g} mm instead of "
+              "1 m, whose candidate search is O(N^2) here) and the every-triangle wall loop culled by a triangle "
+              "grid (same contacts, same order); OpenMP over particles")
     line = {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": len(rates),
-        "warmup": args.warmup_ref, "ms_per_step": 1e3 * t_all / len(rates), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": wl["name"], "describe": wl["describe"], "mode": "parity"},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{len(idx):,} particles nearest the bed centre, all {len(wl['tri_v']):,} "
-                                   "triangles, one step per timed sample; literal reference algorithm"},
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": common_config(wl, ws),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": om.get_threads(), "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -633,23 +1060,20 @@ def run_reference(args, log):
 
 
 def run_ours(args, log):
+    t_start = time.time()
     ws, rank, local = dist_info()
     dist = init_dist(ws)
     import torch
     import rusty_particles_gb300 as rp
     torch.cuda.set_device(local)
+    threads = os.cpu_count() or 1
     wl = make_workload(args)
-    n = len(wl["radius"])
     loaded = None
     if args.state_in:  # a settled state saved by --state-out (positions, velocities, ...)
         loaded = dict(np.load(args.state_in))
         wl["position"] = loaded["position"]
-    elif args.workload in ("hopper", "adhesive", "batched", "drum"):
-        relax(rp, wl, log=log)
-    sim = make_sim(rp, wl, args.mode, args.precision)
-    sim._L.rp_enable_gpu(sim._h, local)
-    if args.host_loop:
-        sim._L.rp_set_device_loop(sim._h, 0)
+    else:
+        prepared(rp, wl, log)
     jkr = None
     if wl["normal"] == "jkr":
         solver = args.jkr_solver or "learned"
@@ -657,137 +1081,84 @@ def run_ours(args, log):
         if solver == "learned":
             if args.jkr_net_in:
                 z = np.load(args.jkr_net_in)
-                sim.set_jkr_network(z["params"], z["norm"], z["domain"])
-                jkr["network"] = f"loaded from {os.path.basename(args.jkr_net_in)}"
+                jkr["network"] = (z["params"], z["norm"], z["domain"])
             else:
-                jkr["training"] = sim.train_jkr_network(seed=1)
+                jkr["network"], _ = jkr_network(rp, wl, {"position": wl["position"], "radius": wl["radius"],
+                                                         "mass": wl["mass"]}, log)
             if args.jkr_net_out:
-                p, nm, dm = sim.get_jkr_network()
+                p, nm, dm = jkr["network"]
                 np.savez(args.jkr_net_out, params=p, norm=nm, domain=dm)
-        sim.set_jkr_solver(solver)
-    # The relaxed start still carries overlaps and an expanded packing that
-    # relax within a few hundred to 2,000 steps under the workload's own
-    # dynamics (step time falls by 1.3-1.6x meanwhile); these untimed settle
-    # steps put the warm-up and the timed steps in the steady state.
+    state = None
+    settle = 0 if loaded is not None else int(wl.get("settle", 0))
     if loaded is not None:
-        sim.set_state({k: v for k, v in loaded.items() if k not in ("radius", "mass", "fixed")})
-    else:
-        settle = int(wl.get("settle", 0))
-        if settle:
-            t_settle = time.time()
-            sim.steps(settle)
-            log(f"settled {settle} steps in {time.time() - t_settle:.1f} s")
+        state = {k: v for k, v in loaded.items()}
     if args.state_out:
-        np.savez(args.state_out, **sim.get_state())
-    sim.steps(args.warmup)
-    tune = None
-    if args.autotune or (args.workload == "batched" and not args.no_autotune):
-        tune = sim.autotune()
-    torch.cuda.synchronize()
-    s0 = sim.stats()
-    c0 = sim.jkr_counters() if jkr else None
-    clocks = ClockSampler(local)
-    barrier(dist)
-    torch.cuda.synchronize()
-    clocks.start()
-    t0 = time.perf_counter()
-    sim.steps(args.steps)  # one device step loop (CUDA graph) for all K steps
-    torch.cuda.synchronize()
-    wall = time.perf_counter() - t0
-    barrier(dist)
-    ck = clocks.stop()
-    s1 = sim.stats()
-    if jkr:
-        c1 = sim.jkr_counters()
-        d = {k: (c1[k] - c0[k]) / args.steps for k in c1}
-        ev = d["accepted"] + d["zero"] + d["fallback"]
-        jkr["per_step"] = d
-        if ev > 0:
-            jkr["fraction"] = {"converging": d["accepted"] / ev, "certified_zero": d["zero"] / ev,
-                               "reference_newton": d["fallback"] / ev}
-    dev_ms = s1["device_ms"] - s0["device_ms"]
-    n_now = s1["particles"]
-    t_max = allreduce_max(dist, dev_ms)
-    total_units = allreduce_sum(dist, n_now * args.steps)
-    value = total_units / (t_max / 1e3)
-    launches = s1["kernel_launches"] - s0["kernel_launches"]
+        sim0 = make_sim(rp, wl, args.mode, args.precision)
+        setup_jkr(sim0, jkr)
+        sim0.steps(settle)
+        np.savez(args.state_out, **sim0.get_state())
+        del sim0
+        settle = 0
+        state = dict(np.load(args.state_out))
     if args.profile_only:
+        sim = make_sim(rp, wl if state is None else wl_at(wl, state), args.mode, args.precision)
+        if args.host_loop:
+            sim._L.rp_set_device_loop(sim._h, 0)
+        setup_jkr(sim, jkr)
+        if state is not None:
+            set_dynamic_state(sim, state)
+        sim.steps(settle + args.warmup)
+        s0, s1, wall, ck = timed(sim, args.steps, dist, local)
         if rank == 0:
-            print(json.dumps({"profile_only": True, "particles": int(n_now), "steps": args.steps,
-                              "ms_per_step": t_max / args.steps, "gpu_launches": int(launches)}), flush=True)
+            print(json.dumps({"profile_only": True, "particles": int(s1["particles"]), "steps": args.steps,
+                              "ms_per_step": (s1["device_ms"] - s0["device_ms"]) / args.steps,
+                              "gpu_launches": int(s1["kernel_launches"] - s0["kernel_launches"])}), flush=True)
         return 0
-    # roofline of the dominant kernel: the same steps issued from the host with
-    # CUDA events around every force launch on the engine's stream
-    sim._L.rp_set_profiling(sim._h, 1)
-    p0 = sim.stats()
-    sim.steps(min(args.steps, 200))
-    p1 = sim.stats()
-    sim._L.rp_set_profiling(sim._h, 0)
-    force_ms = (p1["force_ms"] - p0["force_ms"]) / max(1, p1["force_launches"] - p0["force_launches"])
-    step_ms_profiled = (p1["device_ms"] - p0["device_ms"]) / max(1, p1["steps"] - p0["steps"])
-    # algorithmic bytes per force launch (see B0_FP64)
-    tri = len(wl["tri_v"])
-    alg_bytes = n_now * B0_FP64 + tri * B_TRIANGLE
-    peak, peak_kind = measured_peaks()
-    achieved = alg_bytes / (force_ms / 1e3) / 1e9
-    traffic, fp64_pct = profiled_traffic(wl["name"], n_now)
-    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": traffic,
-            "kernel": ("force pass (k_contact_filter, scans, k_contact_index, k_contact_force, k_accumulate, "
-                       "k_accumulate_walls)"),
-            "fp64_pipe_active_pct": fp64_pct,
-            "avg_launch_ms": force_ms,
-            "force_share_of_step": force_ms / step_ms_profiled if step_ms_profiled > 0 else None,
-            "algorithmic_bytes_per_launch": alg_bytes, "peak_source": peak_kind}
-    # end to end through the public API with host buffers: the inputs and the
-    # result arrays are allocated (and their pages populated) before timing
-    st = sim.get_state()
-    out_buf = {k: np.empty_like(v) for k, v in st.items()}
-    for v in out_buf.values():
-        v.fill(0)
-    e2e_steps = args.steps
-    e0 = sim.stats()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    sim.set_state(st)
-    sim.steps(e2e_steps)
-    sim.get_state(out=out_buf)
-    wall_e2e = time.perf_counter() - t0
-    e2e_device_ms = sim.stats()["device_ms"] - e0["device_ms"]  # the steps(K) call alone
-    h2d = sum(int(v.nbytes) for v in st.values())  # the arrays handed to set_state
-    d2h = sum(int(v.nbytes) for v in out_buf.values())  # the arrays get_state fills
-    e2e_val = allreduce_sum(dist, n * e2e_steps) / allreduce_max(dist, wall_e2e)
-    del out_buf
+    _, res, final = run_form(rp, wl, args, dist, local, log, mode=args.mode, precision=args.precision, jkr=jkr,
+                             state=state, settle=settle, autotune=args.autotune or (
+                                 args.workload == "batched" and not args.no_autotune),
+                             host_loop=args.host_loop)
+    res["roofline"]["traffic"], res["roofline"]["fp64_pipe_active_pct"] = profiled_traffic(wl["name"],
+                                                                                           res["particles"])
     if rank != 0:
         barrier(dist)
         return 0
-    cpu = None if args.no_cpu else cpu_baseline(wl, budget_s=args.cpu_budget)
+    cache = {}
+    ferr = None
+    cpu, cpu_lit = None, None
+    if not args.no_force_err:
+        try:
+            ferr = force_error(rp, wl, final, args.mode, args.precision, jkr, cache, log, threads, keep_oracle=True)
+        except Exception as ex:
+            ferr = {"error": f"{type(ex).__name__}: {ex}"}
+    if not args.no_cpu and "groups" not in wl:
+        cpu, cpu_lit = cpu_baselines(wl, final, cache, threads, args.cpu_budget, log)
+    forms = None
+    if ws == 1 and not args.no_forms and args.workload == "hopper" and args.mode == "parity" \
+            and args.precision == "fp64":
+        got = run_forms(rp, args, dist, local, log, final, wl, cache, threads, t_start + args.forms_budget)
+        forms = {"hopper-1M": {"plain": form_entry(res, ferr), **got.pop("hopper-1M", {})}}
+        forms.update(got)
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if args.precision == "fp64" else "f32-pairs/f64-state", "data": "synthetic",
-        "config": {"workload": wl["name"], "describe": wl["describe"], "particles": int(n_now), "mode": args.mode,
-                   "precision": args.precision, "parallelism": f"replicas x{ws}",
-                   "l2": f"inputs larger than L2 (particle state {n_now * 312 / 1e6:.0f} MB)",
-                   "wall_s_timed": wall},
-        "roofline": roof, "cpu_baseline": cpu,
-        "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d / e2e_steps,
-                "d2h_bytes_per_step": d2h / e2e_steps,
-                "note": ("set_state (H2D of the full state) + steps(K) + get_state(out=...) (D2H into host "
-                         "arrays allocated before timing), K = steps, run after the timed steps"),
-                "device_ms_of_steps": e2e_device_ms, "wall_ms": wall_e2e * 1e3,
-                "transfer": ("kernels on the caller's pageable arrays" if s1.get("state_io_direct")
-                             else "one device copy per array, gather/scatter kernels between id order and the slots")},
-        "gpu_launches": int(launches), "clocks": ck,
-        "stats": {k: s1[k] for k in ("neighbor_rebuilds", "max_neighbors", "neighbor_capacity", "removed")},
+        "metric": METRIC, "value": res["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": res["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32-pairs/f64-state",
+        "data": "synthetic", "config": common_config(wl, ws),
+        "roofline": res["roofline"], "cpu_baseline": cpu, "cpu_baseline_literal": cpu_lit,
+        "e2e": res["e2e"], "gpu_launches": res["gpu_launches"], "clocks": res["clocks"],
+        "force_err": ferr, "precision": args.precision, "wall_s_timed": res["wall_s_timed"],
+        "stats": res["stats"],
     }
-    if jkr:
-        line["config"]["jkr"] = jkr
-    if tune:
-        line["config"]["autotune"] = tune
+    if "jkr" in res:
+        line["jkr"] = res["jkr"]
+    if "autotune" in res:
+        line["autotune"] = res["autotune"]
     if args.workload == "batched":
-        line["config"]["boxes"] = int(len(wl["counts"]))
-        line["config"]["one_at_a_time"] = one_at_a_time(rp, wl, min(args.steps, 100))
+        line["boxes"] = int(len(wl["counts"]))
+        line["one_at_a_time"] = one_at_a_time(rp, wl, min(args.steps, 100))
+    if forms is not None:
+        line["forms"] = forms
+    line["bench_wall_s"] = round(time.time() - t_start, 1)
     print(json.dumps(line), flush=True)
     barrier(dist)
     return 0
@@ -796,8 +1167,8 @@ def run_ours(args, log):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=500)
-    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=["hopper", "box", "adhesive", "batched", "drum"], default="hopper")
     ap.add_argument("--boxes", type=int, default=512, help="boxes of the batched workload")
@@ -809,8 +1180,15 @@ def main():
     ap.add_argument("--jkr-net-out", default=None, help="save the trained JKR network (.npz)")
     ap.add_argument("--mode", choices=["parity", "physical"], default="parity")
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
-    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baselines")
+    ap.add_argument("--no-force-err", action="store_true", help="skip the force error against the oracle")
+    ap.add_argument("--no-forms", action="store_true", help="skip the other forms (headline hopper run only)")
+    ap.add_argument("--forms", default=None, help="comma list of form workloads: hopper,adhesive,drum,batched")
+    ap.add_argument("--forms-budget", type=float, default=600.0,
+                    help="seconds from the start after which no further form starts")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--form-scale", type=float, default=1.0,
+                    help="scale of the other forms' workloads (1 = the benchmark sizes; smaller for quick checks)")
     ap.add_argument("--particles", type=int, default=None,
                     help="workload size (hopper 1,048,576, adhesive 4,194,304 by default)")
     ap.add_argument("--state-in", default=None, help="settled state (.npz from --state-out) instead of relaxing")
@@ -818,8 +1196,6 @@ def main():
     ap.add_argument("--host-loop", action="store_true", help="host-issued kernels instead of the device loop")
     ap.add_argument("--profile-only", action="store_true", help="warm-up + timed steps only (for ncu)")
     args = ap.parse_args()
-    args.steps_ref = max(1, min(args.steps, 10))
-    args.warmup_ref = max(1, min(args.warmup, 2))
     log = (lambda m: print(m, file=sys.stderr, flush=True))
     if args.impl == "reference":
         return run_reference(args, log)

@@ -354,6 +354,19 @@ struct Sim : Base {
   struct Hist { uint64_t tag; V3<T> xi; };
   std::vector<std::vector<Hist>> hist;
 
+  // Optional exact cull of the wall loop (a benchmark-side variant, off by
+  // default): a uniform grid over the triangles, each listed in every cell
+  // that its box grown by the largest radius overlaps. A sphere can only touch
+  // a triangle when its centre lies in that grown box, so the triangles of the
+  // centre's cell, in mesh order, give the same contacts in the same order as
+  // the reference's every-triangle loop (src/simulation.rs:465-466).
+  bool wall_cull = false;
+  size_t cull_T = 0;
+  T cull_rmax = T(-1), cull_h = T(1);
+  V3<T> cull_lo;
+  int cull_d[3] = {0, 0, 0};
+  std::vector<uint32_t> cull_start, cull_items;
+
   // last-step diagnostics
   std::vector<V3<T>> lastF, lastT;
   std::vector<double> lastFS, lastTS;  // sums of |f_contact| and |r x f| per particle (summation-order scale)
@@ -496,6 +509,74 @@ struct Sim : Base {
           size_t idx = (size_t)offs[0][c] + (size_t)offs[1][b] * pg[0] + (size_t)offs[2][a] * pg[0] * pg[1];
           for (uint32_t k = pstart[idx]; k < pstart[idx + 1]; ++k) f(pitems[k]);
         }
+  }
+
+  void build_wall_cull(T rmax_) {
+    const size_t nt = tris.size();
+    cull_T = nt;
+    cull_rmax = rmax_;
+    const T grow = rmax_ * T(1.0001);
+    std::vector<V3<T>> blo(nt), bhi(nt);
+    V3<T> lo(T(1e30), T(1e30), T(1e30)), hi(T(-1e30), T(-1e30), T(-1e30));
+    for (size_t t = 0; t < nt; ++t) {
+      const Triangle<T>& tr = tris[t];
+      V3<T> a(std::min(tr.v0.x, std::min(tr.v1.x, tr.v2.x)), std::min(tr.v0.y, std::min(tr.v1.y, tr.v2.y)),
+              std::min(tr.v0.z, std::min(tr.v1.z, tr.v2.z)));
+      V3<T> b(std::max(tr.v0.x, std::max(tr.v1.x, tr.v2.x)), std::max(tr.v0.y, std::max(tr.v1.y, tr.v2.y)),
+              std::max(tr.v0.z, std::max(tr.v1.z, tr.v2.z)));
+      blo[t] = V3<T>(a.x - grow, a.y - grow, a.z - grow);
+      bhi[t] = V3<T>(b.x + grow, b.y + grow, b.z + grow);
+      lo = V3<T>(std::min(lo.x, blo[t].x), std::min(lo.y, blo[t].y), std::min(lo.z, blo[t].z));
+      hi = V3<T>(std::max(hi.x, bhi[t].x), std::max(hi.y, bhi[t].y), std::max(hi.z, bhi[t].z));
+    }
+    cull_lo = lo;
+    T ext[3] = {hi.x - lo.x, hi.y - lo.y, hi.z - lo.z};
+    T h = std::max(rmax_ * T(2), std::max(ext[0], std::max(ext[1], ext[2])) / T(512));
+    if (!(h > T(0))) h = T(1);
+    for (;;) {
+      uint64_t tot = 1;
+      for (int k = 0; k < 3; ++k) {
+        cull_d[k] = std::max(1, (int)std::ceil(ext[k] / h) + 1);
+        tot *= (uint64_t)cull_d[k];
+      }
+      if (tot <= ((uint64_t)1 << 23)) break;
+      h = h * T(1.5);
+    }
+    cull_h = h;
+    auto range = [&](T v, T o, int k) {
+      int64_t c = (int64_t)std::floor((v - o) / h);
+      return (int)std::max<int64_t>(0, std::min<int64_t>(c, cull_d[k] - 1));
+    };
+    const size_t nc = (size_t)cull_d[0] * cull_d[1] * cull_d[2];
+    cull_start.assign(nc + 1, 0);
+    auto each = [&](size_t t, auto&& f) {
+      int a0 = range(blo[t].x, lo.x, 0), a1 = range(blo[t].y, lo.y, 1), a2 = range(blo[t].z, lo.z, 2);
+      int b0 = range(bhi[t].x, lo.x, 0), b1 = range(bhi[t].y, lo.y, 1), b2 = range(bhi[t].z, lo.z, 2);
+      for (int z = a2; z <= b2; ++z)
+        for (int y = a1; y <= b1; ++y)
+          for (int x = a0; x <= b0; ++x) f((size_t)x + (size_t)cull_d[0] * ((size_t)y + (size_t)cull_d[1] * z));
+    };
+    for (size_t t = 0; t < nt; ++t) each(t, [&](size_t c) { cull_start[c + 1]++; });
+    for (size_t c = 0; c < nc; ++c) cull_start[c + 1] += cull_start[c];
+    cull_items.assign(cull_start[nc], 0);
+    std::vector<uint32_t> fill(cull_start.begin(), cull_start.end() - 1);
+    for (size_t t = 0; t < nt; ++t) each(t, [&](size_t c) { cull_items[fill[c]++] = (uint32_t)t; });
+  }
+  // The culled triangle range of a centre: [s, e) into cull_items, empty
+  // outside the grid (no grown box reaches there).
+  void cull_range(V3<T> x, uint32_t& s, uint32_t& e) const {
+    s = e = 0;
+    T q[3] = {(x.x - cull_lo.x) / cull_h, (x.y - cull_lo.y) / cull_h, (x.z - cull_lo.z) / cull_h};
+    int64_t c[3];
+    for (int k = 0; k < 3; ++k) {
+      if (!(q[k] >= T(0))) return;
+      T f = std::floor(q[k]);
+      if (f >= (T)cull_d[k]) return;
+      c[k] = (int64_t)f;
+    }
+    const size_t idx = (size_t)c[0] + (size_t)cull_d[0] * ((size_t)c[1] + (size_t)cull_d[1] * c[2]);
+    s = cull_start[idx];
+    e = cull_start[idx + 1];
   }
 
   T max_cutoff() const {
@@ -647,6 +728,11 @@ struct Sim : Base {
     // broad phase
     if (mode == MODE_PARITY) { if (grid_dims() != 0) { fprintf(stderr, "oracle: grid too large\n"); return; } build_grid(); }
     else build_physical_grid(max_cutoff());
+    if (wall_cull && !tris.empty()) {
+      T rm = T(0);
+      for (const Particle<T>& p : ps) rm = std::max(rm, p.r);
+      if (cull_T != tris.size() || rm > cull_rmax) build_wall_cull(rm);
+    }
     // 3. per-particle force gather (src/simulation.rs:317-526)
     T es = effective_youngs(pm.E, pm.nu, pm.E, pm.nu);
     T gs = mode == MODE_PARITY ? T(0) : physical_shear(pm.E, pm.nu, pm.E, pm.nu);
@@ -689,7 +775,10 @@ struct Sim : Base {
         });
       }
       // particle-mesh (src/simulation.rs:464-523)
-      for (const Triangle<T>& tr : tris) {
+      uint32_t ts0 = 0, ts1 = (uint32_t)tris.size();
+      if (wall_cull && !tris.empty()) cull_range(p.x, ts0, ts1);
+      for (uint32_t tt = ts0; tt < ts1; ++tt) {
+        const Triangle<T>& tr = tris[wall_cull ? cull_items[tt] : tt];
         T pen; V3<T> nrm, cp;
         if (!intersect_sphere(tr, p.x, p.r, pen, nrm, &cp)) continue;
         if (pen > T(0.2) * p.r) excessive = true;
@@ -821,6 +910,22 @@ void orc_add_particle(void* hv, double x, double y, double z, double r, double m
     s->add_particle(V3<T>((T)x, (T)y, (T)z), (T)r, (T)m, fixed != 0);
     return 0;
   });
+}
+// Bulk form of orc_add_particle: xyz 3n doubles, r and m n doubles, fixed n bytes (may be null).
+void orc_add_particles(void* hv, long n, const double* xyz, const double* r, const double* m, const unsigned char* fixed) {
+  dispatch((Handle*)hv, [&](auto* s) {
+    using T = decltype(s->dt);
+    s->ps.reserve(s->ps.size() + (size_t)n);
+    for (long i = 0; i < n; ++i)
+      s->add_particle(V3<T>((T)xyz[3 * i], (T)xyz[3 * i + 1], (T)xyz[3 * i + 2]), (T)r[i], (T)m[i],
+                      fixed ? fixed[i] != 0 : false);
+    return 0;
+  });
+}
+// Benchmark-side variant: cull the wall loop by a triangle grid (same contacts,
+// same order as the every-triangle loop; off by default).
+void orc_set_wall_cull(void* hv, int on) {
+  dispatch((Handle*)hv, [&](auto* s) { s->wall_cull = on != 0; s->cull_T = 0; return 0; });
 }
 // v: 9 doubles per triangle (v0,v1,v2), nrm: 3 doubles per triangle
 void orc_add_triangles(void* hv, const double* v, const double* nrm, long nt) {

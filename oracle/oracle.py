@@ -59,6 +59,8 @@ def lib():
             "orc_get_threads": (i, []),
             "orc_add_particle": (None, [vp, d, d, d, d, d, i]),
             "orc_add_triangles": (None, [vp, dp, dp, l]),
+            "orc_add_particles": (None, [vp, l, dp, dp, dp, ctypes.POINTER(ctypes.c_ubyte)]),
+            "orc_set_wall_cull": (None, [vp, i]),
             "orc_add_triangles_moving": (None, [vp, dp, dp, l, dp]),
             "orc_set_material": (None, [vp, i, d, d, d, d, d, d]),
             "orc_set_models": (None, [vp, i, i]),
@@ -173,6 +175,22 @@ class OracleSimulation:
 
     def add_particle(self, x, y, z, radius, mass, fixed=False):
         self._L.orc_add_particle(self._h, x, y, z, radius, mass, 1 if fixed else 0)
+
+    def add_particles(self, xyz, r, m, fixed=None):
+        """Bulk add: positions [N,3], radii [N], masses [N], fixed flags [N] (optional)."""
+        xyz = np.ascontiguousarray(xyz, np.float64).reshape(-1, 3)
+        r = np.ascontiguousarray(r, np.float64).reshape(-1)
+        m = np.ascontiguousarray(m, np.float64).reshape(-1)
+        fx = None
+        if fixed is not None:
+            fx = np.ascontiguousarray(fixed, np.uint8).reshape(-1)
+        self._L.orc_add_particles(self._h, len(xyz), _dp(xyz), _dp(r), _dp(m),
+                                  fx.ctypes.data_as(ctypes.POINTER(ctypes.c_ubyte)) if fx is not None else None)
+
+    def set_wall_cull(self, on=True):
+        """Cull the wall loop by a triangle grid: the contacts and their order
+        are those of the reference's every-triangle loop (a baseline variant)."""
+        self._L.orc_set_wall_cull(self._h, 1 if on else 0)
 
     def add_mesh(self, path):
         v, n = read_stl(path)
