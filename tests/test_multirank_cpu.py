@@ -44,7 +44,7 @@ def _reductions(rank, port, q):
 def _reference_arm(rank, port, q):
     _env(rank, port)
     import bench
-    args = argparse.Namespace(workload="box", particles=None, boxes=512, steps_ref=1, warmup_ref=1)
+    args = argparse.Namespace(workload="box", particles=None, boxes=512, steps=1, warmup=1)
     buf = io.StringIO()
     with redirect_stdout(buf):
         rc = bench.run_reference(args, lambda m: None)
