@@ -542,6 +542,34 @@ def profiled_traffic(workload_name, n):
         return None, None
 
 
+def fp64_roofline(rp, wl, n, ms_per_step):
+    """The step against the FP64 pipe: the device's FP64 rate measured now by
+    librp (rp_measure_fp64_peak), the FP64-pipe thread instructions per
+    particle-step counted by ncu on a smaller bed of the same workload
+    (profiles/fp64_ops_<workload>.json), and the fraction of that rate the
+    timed step reaches."""
+    import ctypes
+    from rusty_particles_gb300 import _lib
+    fma, add = ctypes.c_double(), ctypes.c_double()
+    if _lib.load().rp_measure_fp64_peak(ctypes.byref(fma), ctypes.byref(add)) != 0:
+        return None
+    out = {"peak_fma_per_s": fma.value, "peak_add_per_s": add.value, "unit": "FP64 thread instructions/s",
+           "peak_source": "measured in this run (librp rp_measure_fp64_peak, CUDA events)"}
+    p = os.path.join(ROOT, "profiles", f"fp64_ops_{wl['name']}.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        per = float(d["fp64_pipe_inst_per_particle_step"])
+    except (OSError, KeyError, ValueError):
+        return out
+    achieved = per * n / (ms_per_step / 1e3)
+    out.update({"fp64_pipe_inst_per_particle_step": per,
+                "dadd_dmul_dfma_per_particle_step": d.get("dadd_dmul_dfma_per_particle_step"),
+                "achieved": achieved, "frac": achieved / fma.value,
+                "counts_source": d.get("source")})
+    return out
+
+
 # ------------------------------------------------------ CPU side (the oracle)
 STATE_VEC = ("position", "velocity", "angular_velocity", "acceleration", "torque", "position_residual",
              "velocity_residual", "angular_velocity_residual")
@@ -1120,6 +1148,7 @@ def run_ours(args, log):
                              host_loop=args.host_loop)
     res["roofline"]["traffic"], res["roofline"]["fp64_pipe_active_pct"] = profiled_traffic(wl["name"],
                                                                                            res["particles"])
+    res["roofline"]["fp64"] = fp64_roofline(rp, wl, res["particles"], res["ms_per_step"])
     if rank != 0:
         barrier(dist)
         return 0

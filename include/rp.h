@@ -98,6 +98,10 @@ typedef struct rp_stats {
                                   the caller's pageable arrays (the device reaches host memory through
                                   the host page tables; opt-in, RP_DIRECT_STATE_IO=1); 0: staged
                                   device copies (default) */
+  uint64_t state_uploads;      /* full host->device uploads of the particle state (first step, host edits) */
+  uint64_t state_downloads;    /* full device->host downloads of the particle state (per-particle getters) */
+  uint64_t compactions;        /* removals compacted on the device (no host round trip) */
+  uint64_t device_inserts;     /* particles appended to the device slots without a host round trip */
 } rp_stats;
 
 #define RP_STATUS_OVERLAP 1u    /* overlap > 20 % of the smaller radius (src/simulation.rs:361-370) */
@@ -183,6 +187,12 @@ int rp_get_stats(rp_sim* sim, rp_stats* out);
 int rp_set_profiling(rp_sim* sim, int enable);
 const char* rp_last_error(void);
 const char* rp_version(void);
+
+/* FP64 throughput of the current device, measured with CUDA events (thread
+ * instructions per second of FP64 fused multiply-add and of FP64 addition,
+ * eight independent chains per thread, best of three launches): the ceiling of
+ * the FP64-bound kernels of the step. No reference counterpart. */
+int rp_measure_fp64_peak(double* fma_per_s, double* add_per_s);
 
 /* --- diagnostics for parity checks (no reference counterpart) */
 /* Record per-particle force/torque and contact multiplicities during steps. */

@@ -62,6 +62,10 @@ class RpStats(ctypes.Structure):
         ("force_launches", ctypes.c_uint64),
         ("force_ms", ctypes.c_double),
         ("state_io_direct", ctypes.c_uint64),
+        ("state_uploads", ctypes.c_uint64),
+        ("state_downloads", ctypes.c_uint64),
+        ("compactions", ctypes.c_uint64),
+        ("device_inserts", ctypes.c_uint64),
     ]
 
 
@@ -154,6 +158,7 @@ SIGNATURES = {
     "rp_set_force_path": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "rp_set_threads": (ctypes.c_int, [ctypes.c_int]),
     "rp_get_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(RpStats)]),
+    "rp_measure_fp64_peak": (ctypes.c_int, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     "rp_set_profiling": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "rp_last_error": (ctypes.c_char_p, []),
     "rp_version": (ctypes.c_char_p, []),

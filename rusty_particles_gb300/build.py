@@ -23,7 +23,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=o
 # Per-file extra flags: the step kernels and the JKR sample generator must not
 # fuse multiply-adds (their rounding has to match the oracle's).
 EXTRA = {"k_step.cu": ["-fmad=false"], "k_mlp.cu": ["-fmad=false"]}
-SOURCES = ["k_broadphase.cu", "k_step.cu", "engine.cu", "rp_api.cu", "k_noalloc.cu", "k_mlp.cu"]
+SOURCES = ["k_broadphase.cu", "k_step.cu", "engine.cu", "rp_api.cu", "k_noalloc.cu", "k_mlp.cu", "k_fp64.cu"]
 
 
 def nvcc() -> str:

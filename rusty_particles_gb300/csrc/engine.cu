@@ -543,7 +543,12 @@ int Engine::build_params() {
     }
     P.rdims[k] = (int)q + 1;
   }
-  // fine grid: cell >= largest list radius
+  // two particles in the same inserted reference cell: each axis lists that
+  // cell once, or three times on a periodic axis of a single cell (the -1, 0
+  // and +1 offsets all wrap onto it), src/grid.rs:54-85
+  P.same_cell_visits = 1;
+  for (int k = 0; k < 3; ++k)
+    if (periodic[k] && P.rdims[k] == 1) P.same_cell_visits *= 3;
   double rmax = 0.0;
   for (const HostParticle& p : hp_) rmax = std::max(rmax, p.r);
   const double adh = (nmodel == RP_NORMAL_JKR || nmodel == RP_NORMAL_SJKR) ? 1.5 : 1.0;
@@ -819,6 +824,10 @@ int Engine::upload() {
   }
   up_tags_.resize(n);
   for (size_t i = 0; i < n; ++i) up_tags_[i] = hp_[i].tag;
+  n_upload_ = (int)n;
+  rmax_dev_ = 0.0;
+  for (size_t i = 0; i < n; ++i) rmax_dev_ = std::max(rmax_dev_, hp_[i].r);
+  ++uploads_;
   Bank& B = bank_[0];
   D4* dst[8] = {B.xr, B.vm, B.wc, B.acc, B.tq, B.xres, B.vres, B.wres};
   if (n > 0) {
@@ -863,6 +872,7 @@ int Engine::download() {
   }
   CK(cudaSetDevice(device_));
   TRY(sync_ctrl());
+  ++downloads_;
   const Bank& B = bank_[ctrl_h_->bank];
   const size_t n = (size_t)n_;
   std::vector<D4> a8[8];
@@ -1120,10 +1130,135 @@ int Engine::step(uint64_t n) {
   launches_ += launch_second_half(P_, stream_);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(stream_));
-  // many removals: compact through the host before the next step
-  if (last_.removed > 0 && last_.removed * 8 > (uint64_t)n_) {
-    TRY(download());
+  if (last_.removed > 0) TRY(compact_removed());
+  return RP_OK;
+}
+
+// Removed particles leave the slots on the device (src/simulation.rs:199-219
+// drops them and re-indexes the rest). A rebuild of the lists sorts every
+// slot by its fine-grid cell, and a dead slot's key lies past every cell, so
+// after it the live slots are exactly [0, n_live): dropping the dead ones is
+// setting the slot count. The ids of the live particles keep coming from the
+// scan of the live flags over the upload positions (launch_slot_of), which is
+// the reference's re-indexing in insertion order. The next step rebuilds the
+// lists and the visiting order for the new count.
+int Engine::compact_removed() {
+  TRY(sync_ctrl());
+  const uint64_t dead = ctrl_h_->removed;
+  if (dead == 0 || ctrl_h_->halt) return RP_OK;
+  for (int tries = 0;; ++tries) {
+    const int one = 1;
+    CK(cudaMemcpyAsync(&ctrl_->rebuild, &one, sizeof(int), cudaMemcpyHostToDevice, stream_));
+    launches_ += launch_rebuild(P_, rb_, stream_);
+    CK(cudaGetLastError());
+    TRY(sync_ctrl());
+    if (!ctrl_h_->halt) break;
+    if (tries >= 8) {
+      set_error("neighbour lists keep overflowing while compacting removed particles");
+      return RP_E_DEVICE_FLAG;
+    }
+    // a list outgrew its capacity in that rebuild (the bank did not flip):
+    // grow the lists and run the rebuild again from the same bank
+    const int newcap = std::max<int>(cap_ + 8, (int)(ctrl_h_->max_count * 5 / 4 + 8));
+    TRY(alloc_lists(newcap, true));
+    tot_.status |= ST_NLIST_GROW;
+    const int zero = 0;
+    const unsigned zu = 0;
+    CK(cudaMemcpyAsync(&ctrl_->halt, &zero, sizeof(int), cudaMemcpyHostToDevice, stream_));
+    CK(cudaMemcpyAsync(&ctrl_->max_count, &zu, sizeof(unsigned), cudaMemcpyHostToDevice, stream_));
   }
+  tot_.rebuilds += ctrl_h_->rebuilds - last_.rebuilds;
+  n_ -= (int)dead;
+  P_.n = n_;
+  const unsigned long long zero64 = 0;
+  const int one = 1;
+  CK(cudaMemcpyAsync(&ctrl_->removed, &zero64, sizeof(zero64), cudaMemcpyHostToDevice, stream_));
+  CK(cudaMemcpyAsync(&ctrl_->rebuild, &one, sizeof(int), cudaMemcpyHostToDevice, stream_));
+  TRY(sync_ctrl());
+  last_ = *ctrl_h_;
+  graph_dirty_ = true;  // the slot count is a kernel parameter
+  ++compactions_;
+  return RP_OK;
+}
+
+// Insertion while the device holds the state (src/simulation.rs:93-96 pushes
+// to the end of the particle list): the new particles take the slots after the
+// live ones in the current bank, with upload positions after every existing
+// one (so their ids follow all current ids), and the next step rebuilds the
+// lists. Applies when the slots have room and the new radii do not exceed the
+// largest uploaded radius (the grids are sized by it); otherwise the caller
+// takes the host path (a fresh upload).
+int Engine::append_on_device(size_t k, const double* xyz, const double* r, const double* m, const uint8_t* fixed,
+                             bool& done) {
+  done = false;
+  if (!gpu_ || !dev_valid_ || k == 0 || P_.ngroups > 1) return RP_OK;
+  if ((size_t)n_ + k > n_alloc_ || (size_t)n_upload_ + k > (size_t)0x7FFFFFF0) return RP_OK;
+  for (size_t i = 0; i < k; ++i)
+    if (!(r[i] > 0.0) || !(m[i] > 0.0) || r[i] > rmax_dev_) return RP_OK;
+  CK(cudaSetDevice(device_));
+  TRY(sync_ctrl());
+  if (ctrl_h_->halt || ctrl_h_->pending || ctrl_h_->removed) return RP_OK;
+  std::vector<D4> a8[8];
+  for (auto& v : a8) v.assign(k, D4{0.0, 0.0, 0.0, 0.0});
+  std::vector<uint32_t> flags(k), tags(k), zero(k, 0u);
+  std::vector<float4> xf(k), xref(k, make_float4(NAN, NAN, NAN, 0.f));
+  for (size_t i = 0; i < k; ++i) {
+    a8[0][i] = D4{xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], r[i]};
+    a8[1][i] = D4{0.0, 0.0, 0.0, m[i]};
+    a8[6][i] = D4{0.0, 0.0, 0.0, 1.0 / m[i]};
+    a8[7][i] = D4{0.0, 0.0, 0.0, 1.0 / (0.4 * m[i] * r[i] * r[i])};
+    flags[i] = (fixed && fixed[i]) ? PF_FIXED : 0u;
+    tags[i] = (uint32_t)(n_upload_ + i);
+    xf[i] = make_float4((float)xyz[3 * i], (float)xyz[3 * i + 1], (float)xyz[3 * i + 2], (float)r[i]);
+  }
+  const Bank& B = bank_[ctrl_h_->bank];
+  D4* dst[8] = {B.xr, B.vm, B.wc, B.acc, B.tq, B.xres, B.vres, B.wres};
+  const size_t o = (size_t)n_;
+  for (int q = 0; q < 8; ++q)
+    CK(cudaMemcpyAsync(dst[q] + o, a8[q].data(), sizeof(D4) * k, cudaMemcpyHostToDevice, stream_));
+  CK(cudaMemcpyAsync(B.flags + o, flags.data(), sizeof(uint32_t) * k, cudaMemcpyHostToDevice, stream_));
+  CK(cudaMemcpyAsync(B.tag + o, tags.data(), sizeof(uint32_t) * k, cudaMemcpyHostToDevice, stream_));
+  CK(cudaMemcpyAsync(B.grp + o, zero.data(), sizeof(uint32_t) * k, cudaMemcpyHostToDevice, stream_));
+  CK(cudaMemcpyAsync(B.xf + o, xf.data(), sizeof(float4) * k, cudaMemcpyHostToDevice, stream_));
+  CK(cudaMemcpyAsync(B.xref + o, xref.data(), sizeof(float4) * k, cudaMemcpyHostToDevice, stream_));
+  for (int b = 0; b < 2; ++b)
+    CK(cudaMemcpyAsync(bank_[b].ncnt + o, zero.data(), sizeof(uint32_t) * k, cudaMemcpyHostToDevice, stream_));
+  {  // the visiting order of the force kernels covers the new slots until the rebuild
+    std::vector<uint32_t> ids(k);
+    for (size_t i = 0; i < k; ++i) ids[i] = (uint32_t)(o + i);
+    CK(cudaMemcpyAsync(aorder_ + o, ids.data(), sizeof(uint32_t) * k, cudaMemcpyHostToDevice, stream_));
+  }
+  const int one = 1;
+  CK(cudaMemcpyAsync(&ctrl_->rebuild, &one, sizeof(int), cudaMemcpyHostToDevice, stream_));
+  CK(cudaStreamSynchronize(stream_));
+  for (size_t i = 0; i < k; ++i) {
+    up_tags_.push_back(next_tag_);
+    if (host_valid_) {
+      HostParticle p;
+      std::memset(&p, 0, sizeof(p));
+      for (int a = 0; a < 3; ++a) p.x[a] = xyz[3 * i + a];
+      p.r = r[i];
+      p.m = m[i];
+      p.fixed = (fixed && fixed[i]) ? 1 : 0;
+      p.tag = next_tag_;
+      hp_.push_back(p);
+    }
+    ++next_tag_;
+  }
+  n_ += (int)k;
+  n_upload_ += (int)k;
+  P_.n = n_;
+  graph_dirty_ = true;
+  device_inserts_ += k;
+  done = true;
+  return RP_OK;
+}
+
+int Engine::add_particles(size_t k, const double* xyz, const double* r, const double* m, const uint8_t* fixed) {
+  bool done = false;
+  TRY(append_on_device(k, xyz, r, m, fixed, done));
+  if (done) return RP_OK;
+  for (size_t i = 0; i < k; ++i) TRY(add_particle(xyz + 3 * i, r[i], m[i], fixed ? fixed[i] : 0));
   return RP_OK;
 }
 
@@ -1206,10 +1341,11 @@ int Engine::fast_read_state(rp_state* st, bool& done) {
   TRY(sync_ctrl());
   if (ctrl_h_->halt != 0) return RP_OK;
   const size_t n = (size_t)n_ - (size_t)ctrl_h_->removed;  // ids of the live particles
-  TRY(ensure_io((size_t)n_));
+  TRY(ensure_io((size_t)std::max(n_, n_upload_)));
   double* vec[8] = {st->position, st->velocity, st->angular_velocity, st->acceleration,
                     st->torque, st->position_residual, st->velocity_residual, st->angular_velocity_residual};
-  const uint32_t* ids = launch_slot_of(P_, IdMap{slot_of_, id_live_, id_pos_, slot_of_id_, id_part_}, (int)n, stream_);
+  const uint32_t* ids =
+      launch_slot_of(P_, IdMap{slot_of_, id_live_, id_pos_, slot_of_id_, id_part_}, (int)n, n_upload_, stream_);
   if (io_direct_) {  // the gather writes the caller's arrays
     std::vector<std::pair<char*, size_t>> ranges;
     for (int q = 0; q < 8; ++q)
@@ -1251,11 +1387,12 @@ int Engine::fast_write_state(const rp_state* st, bool& done) {
   TRY(sync_ctrl());
   if (ctrl_h_->halt != 0) return RP_OK;
   const size_t n = (size_t)n_ - (size_t)ctrl_h_->removed;  // ids of the live particles
-  TRY(ensure_io((size_t)n_));
+  TRY(ensure_io((size_t)std::max(n_, n_upload_)));
   double* const vec[8] = {st->position, st->velocity, st->angular_velocity, st->acceleration,
                           st->torque, st->position_residual, st->velocity_residual, st->angular_velocity_residual};
   StateIO io{};
-  const uint32_t* ids = launch_slot_of(P_, IdMap{slot_of_, id_live_, id_pos_, slot_of_id_, id_part_}, (int)n, stream_);
+  const uint32_t* ids =
+      launch_slot_of(P_, IdMap{slot_of_, id_live_, id_pos_, slot_of_id_, id_part_}, (int)n, n_upload_, stream_);
   if (io_direct_) {  // the kernels read the caller's arrays
     for (int q = 0; q < 8; ++q) io.v[q] = vec[q];
     io.radius = st->radius;
@@ -1348,6 +1485,10 @@ int Engine::stats(rp_stats* s) {
   s->force_launches = force_launches_;
   s->force_ms = force_ms_;
   s->state_io_direct = io_direct_ ? 1u : 0u;
+  s->state_uploads = uploads_;
+  s->state_downloads = downloads_;
+  s->compactions = compactions_;
+  s->device_inserts = device_inserts_;
   if (gpu_ && dev_valid_ && n_ > 0) {
     CK(cudaSetDevice(device_));
     launch_kinetic_energy(P_, ke_, stream_);

@@ -48,6 +48,9 @@ class Engine {
   int force_path = 0;  // 0 contact-parallel, 1 one thread per particle
 
   int add_particle(const double x[3], double r, double m, int fixed);
+  // n particles at once; appended to the device slots without a host round
+  // trip while the device holds the state (see append_on_device)
+  int add_particles(size_t n, const double* xyz, const double* r, const double* m, const uint8_t* fixed);
   int add_triangles(size_t n, const float* v, const float* nrm, uint32_t group = GROUP_ALL,
                     const WallMotion* motion = nullptr);
   // groups: independent beds stepped together
@@ -166,6 +169,13 @@ class Engine {
   int ensure_gpu();
   int upload();
   int download();
+  // device-side removal and insertion (src/simulation.rs:199-219, 93-96)
+  int compact_removed();
+  int append_on_device(size_t n, const double* xyz, const double* r, const double* m, const uint8_t* fixed,
+                       bool& done);
+  int n_upload_ = 0;          // upload positions (device tags index them); > n_ after compactions
+  double rmax_dev_ = 0.0;     // largest radius of the uploaded set (sizes the grids)
+  uint64_t uploads_ = 0, downloads_ = 0, compactions_ = 0, device_inserts_ = 0;
   // bulk state in id order straight between the caller's arrays and the slots
   // (valid device state, no dead slot); `done` is false when it does not apply
   int fast_read_state(rp_state* st, bool& done);

@@ -298,6 +298,7 @@ __device__ __forceinline__ bool pair_contact(const StepParams& P, const Law& L, 
   constexpr bool F32 = sizeof(R) == sizeof(float);
   R overlap;
   T3<R> n;
+  V nd;  // the unit normal in FP64 (FP32 form: to ~1e-14, for the relative velocity below)
   if (sizeof(R) == sizeof(double)) {
     const double dist = sqrt(d2);
     overlap = (R)(rsum - dist);
@@ -313,9 +314,14 @@ __device__ __forceinline__ bool pair_contact(const StepParams& P, const Law& L, 
     else if (d2 < 0.999e-12) far_enough = false;
     else far_enough = sqrt(d2) > 1e-6;  // exact FP64 decision near the threshold
     if (far_enough) {
-      const float inv = 1.0f / dist;
-      n = T3<R>{(R)((float)d.x * inv), (R)((float)d.y * inv), (R)((float)d.z * inv)};
+      // 1/|d| from the FP32 reciprocal square root and one FP64 Newton step
+      // (relative error ~1e-14, no FP64 square root or division)
+      const double r0 = (double)rsqrtf((float)d2);
+      const double inv = r0 * (1.5 - (0.5 * d2) * (r0 * r0));
+      nd = d * inv;
+      n = cvt<R>(nd);
     } else {
+      nd = vmk(0.0, 1.0, 0.0);
       n = t3(R(0), R(1), R(0));
     }
   }
@@ -329,7 +335,15 @@ __device__ __forceinline__ bool pair_contact(const StepParams& P, const Law& L, 
     const T3<R> vb = cvt<R>(vj) + cross(cvt<R>(wj), rb);
     rv = va - vb;
   } else {
-    rv = cvt<R>(vi - vj) + cross(cvt<R>(wi), ra) - cross(cvt<R>(wj), rb);
+    // In a rolling or sticking contact, and along the normal, the relative
+    // velocity at the contact point is a small difference of large terms
+    // (the spin terms w x r): rounded in FP32 they would swamp the normal
+    // speed of the damping and the slip direction of the friction. So it is
+    // formed in FP64, as (v_i - v_j) - (w_i r_i + w_j r_j) x n (the same
+    // quantity as va - vb with r_a = -n r_i, r_b = n r_j), and only then
+    // rounded for the FP32 laws.
+    const V W = wi * ri + wj * rj;
+    rv = cvt<R>((vi - vj) - cross(W, nd));
   }
   const R rs = (rir * rjr) / (rir + rjr);
   const R ms = ((R)mi * (R)mj) / ((R)mi + (R)mj);
@@ -351,6 +365,14 @@ __device__ __forceinline__ bool pair_contact(const StepParams& P, const Law& L, 
   }
   if (jkind != JKR_FALLBACK) {
   } else if (F32 && P.nmodel == 3) {
+    // The contact radius has a square-root fold next to the pull-off: there
+    // the FP32 iteration cannot resolve the root (an FP32 residual moves it by
+    // ~sqrt(1e-7) relative) and the pair is evaluated in FP64. Elsewhere the
+    // certificates bound the slope away from zero.
+    if (L.gamma_pp > 0.0) {
+      const float x = (float)overlap / (float)rs, c = L.jkr_Cf / (float)rs;
+      if (jkr_certify(x, c, jkr_c23(c), overlap > R(0)) == JKR_FALLBACK) return false;
+    }
     bool near = false;
     fmag = jkr_mag<R>(overlap, (R)L.es_pp, rs, (R)L.gamma_pp, &near);
     if (near) return false;
@@ -457,6 +479,16 @@ __device__ __forceinline__ void second_half_kick(V& v, V& vres, V& w, V& wres, V
 // drift + angular half kick. Also records the reference-grid cell code and
 // requests a list rebuild when a particle moved more than half the skin since
 // the last build.
+//
+// KAHAN = false is the mixed form's integrator: the same velocity-Verlet
+// halves in plain FP64 (v += a dt/2, x += v dt, omega += (tau/I) dt/2), with
+// the reference's Kahan residuals neither read nor updated. From zero
+// residuals one step gives the same bits as the compensated form; over many
+// steps positions and velocities differ from it by FP64 rounding (about one
+// ulp per step), far below the FP32 pair forces' 1e-5. It takes ~60 of the
+// ~85 FP64 operations per particle and 128 of the 484 bytes (the residuals'
+// read and three writes) off this kernel.
+template <bool KAHAN>
 __global__ void __launch_bounds__(256) k_first_half(StepParams P) {
   Ctrl* C = P.ctrl;
   if (C->halt) return;
@@ -484,17 +516,24 @@ __global__ void __launch_bounds__(256) k_first_half(StepParams P) {
       const V a = xyz(B.acc[k]);
       const V tau = xyz(B.tq[k]);
       const D4 vr4 = B.vres[k];
-      vres = xyz(vr4);
       inv_mass = vr4.w;
       const D4 wr4 = B.wres[k];
-      wres = xyz(wr4);
       inv_inertia = wr4.w;
-      xres = xyz(B.xres[k]);
+      if (KAHAN) {
+        vres = xyz(vr4);
+        wres = xyz(wr4);
+        xres = xyz(B.xres[k]);
+      }
       dv = a * hdt;
       dw = (tau * inv_inertia) * hdt;
       if (FUSE) {
-        kahan_add(v, vres, dv);
-        kahan_add(w, wres, dw);
+        if (KAHAN) {
+          kahan_add(v, vres, dv);
+          kahan_add(w, wres, dw);
+        } else {
+          v = v + dv;
+          w = w + dw;
+        }
       }
     }
     if (anyp) {
@@ -516,13 +555,19 @@ __global__ void __launch_bounds__(256) k_first_half(StepParams P) {
       continue;
     }
     if (moving) {
-      kahan_add(v, vres, dv);
-      kahan_add(x, xres, v * dt);
-      kahan_add(w, wres, dw);
+      if (KAHAN) {
+        kahan_add(v, vres, dv);
+        kahan_add(x, xres, v * dt);
+        kahan_add(w, wres, dw);
+        B.vres[k] = D4{vres.x, vres.y, vres.z, inv_mass};
+        B.xres[k] = D4{xres.x, xres.y, xres.z, 0.0};
+        B.wres[k] = D4{wres.x, wres.y, wres.z, inv_inertia};
+      } else {
+        v = v + dv;
+        x = x + v * dt;
+        w = w + dw;
+      }
       B.vm[k] = D4{v.x, v.y, v.z, vm.w};
-      B.vres[k] = D4{vres.x, vres.y, vres.z, inv_mass};
-      B.xres[k] = D4{xres.x, xres.y, xres.z, 0.0};
-      B.wres[k] = D4{wres.x, wres.y, wres.z, inv_inertia};
       wc.x = w.x; wc.y = w.y; wc.z = w.z;
     }
     const float4 xf = make_float4((float)x.x, (float)x.y, (float)x.z, (float)xr.w);
@@ -547,7 +592,8 @@ __global__ void __launch_bounds__(256) k_first_half(StepParams P) {
 }
 
 // Completes the last step of a stepping call (the pending second half);
-// k_clear_pending then marks the state complete.
+// k_clear_pending then marks the state complete. KAHAN as in k_first_half.
+template <bool KAHAN>
 __global__ void __launch_bounds__(256) k_second_half(StepParams P) {
   Ctrl* C = P.ctrl;
   if (C->halt || !C->pending) return;
@@ -558,11 +604,17 @@ __global__ void __launch_bounds__(256) k_second_half(StepParams P) {
     D4 vm = B.vm[k], wc = B.wc[k];
     const D4 wr4 = B.wres[k], vr4 = B.vres[k];
     V v = xyz(vm), w = xyz(wc), vres = xyz(vr4), wres = xyz(wr4);
-    second_half_kick(v, vres, w, wres, xyz(B.acc[k]), xyz(B.tq[k]), wr4.w, P.dt);
+    if (KAHAN) {
+      second_half_kick(v, vres, w, wres, xyz(B.acc[k]), xyz(B.tq[k]), wr4.w, P.dt);
+      B.vres[k] = D4{vres.x, vres.y, vres.z, vr4.w};
+      B.wres[k] = D4{wres.x, wres.y, wres.z, wr4.w};
+    } else {
+      const double hdt = 0.5 * P.dt;
+      v = v + xyz(B.acc[k]) * hdt;
+      w = w + (xyz(B.tq[k]) * wr4.w) * hdt;
+    }
     B.vm[k] = D4{v.x, v.y, v.z, vm.w};
     B.wc[k] = D4{w.x, w.y, w.z, wc.w};
-    B.vres[k] = D4{vres.x, vres.y, vres.z, vr4.w};
-    B.wres[k] = D4{wres.x, wres.y, wres.z, wr4.w};
   }
 }
 
@@ -944,6 +996,9 @@ __global__ void __launch_bounds__(256) k_contact_filter(StepParams P) {
     uint32_t nrec = 0, ncmp = 0, nnet = 0;
     if (!(B.flags[k] & PF_DEAD)) {
       const unsigned long long ci = PHYS ? 0ull : (unsigned long long)__double_as_longlong(B.wc[k].w);
+      // visits of a neighbour in the same reference cell (most pairs at a 1 m
+      // cell): a constant, without the 27-cell walk of ref_visits
+      const int same = (PHYS || !ref_inside(P, ci)) ? 0 : P.same_cell_visits;
       const Law lw = law_of(P, B, k);  // pairs never cross groups (the lists exclude them)
       const bool adhesive = lw.gamma_pp > 0.0;
       const bool learn = learn_any && adhesive, zdrop = zdrop_any && adhesive;
@@ -963,8 +1018,12 @@ __global__ void __launch_bounds__(256) k_contact_filter(StepParams P) {
             vij = vji = 1;
           } else {
             const unsigned long long cj = (unsigned long long)__double_as_longlong(B.wc[j].w);
-            vij = ref_visits(P, ci, cj);
-            vji = ref_visits(P, cj, ci);
+            if (cj == ci) {
+              vij = vji = same;
+            } else {
+              vij = ref_visits(P, ci, cj);
+              vji = ref_visits(P, cj, ci);
+            }
           }
         }
         if (vij > 0) {
@@ -1521,13 +1580,15 @@ __global__ void k_kinetic(StepParams P, double* out) {
 
 int launch_first_half(const StepParams& P, cudaStream_t s) {
   if (P.n == 0) return 0;
-  k_first_half<<<grid_for(P.n, 256), 256, 0, s>>>(P);
+  if (P.prec == 1) k_first_half<false><<<grid_for(P.n, 256), 256, 0, s>>>(P);
+  else k_first_half<true><<<grid_for(P.n, 256), 256, 0, s>>>(P);
   return 1;
 }
 
 int launch_second_half(const StepParams& P, cudaStream_t s) {
   if (P.n == 0) return 0;
-  k_second_half<<<grid_for(P.n, 256), 256, 0, s>>>(P);
+  if (P.prec == 1) k_second_half<false><<<grid_for(P.n, 256), 256, 0, s>>>(P);
+  else k_second_half<true><<<grid_for(P.n, 256), 256, 0, s>>>(P);
   k_clear_pending<<<1, 1, 0, s>>>(P);
   return 2;
 }
@@ -1580,9 +1641,11 @@ static int launch_contact_path(const StepParams& P, cudaStream_t s) {
   else if (hist) k_contact_force<true, true, R><<<gc, bc, 0, s>>>(P);
   else k_contact_force<true, false, R><<<gc, bc, 0, s>>>(P);
   if (P.jfb != nullptr) {
-    if (P.mode == 0) k_contact_deferred<false, false, R><<<P.nsm * 8, 128, 0, s>>>(P);
-    else if (hist) k_contact_deferred<true, true, R><<<P.nsm * 8, 128, 0, s>>>(P);
-    else k_contact_deferred<true, false, R><<<P.nsm * 8, 128, 0, s>>>(P);
+    // the deferred pairs lie in the band next to the JKR fold, where only
+    // FP64 resolves the contact radius: FP64 in the mixed form too
+    if (P.mode == 0) k_contact_deferred<false, false, double><<<P.nsm * 8, 128, 0, s>>>(P);
+    else if (hist) k_contact_deferred<true, true, double><<<P.nsm * 8, 128, 0, s>>>(P);
+    else k_contact_deferred<true, false, double><<<P.nsm * 8, 128, 0, s>>>(P);
     ++launched;
   }
   k_accumulate<<<shaped_grid((uint64_t)P.n, ba, cap), ba, 0, s>>>(P);
@@ -1696,12 +1759,14 @@ __global__ void k_state_scatter(StepParams P, const uint32_t* slot_of, StateIO i
   }
 }
 
-const uint32_t* launch_slot_of(const StepParams& P, const IdMap& M, int live, cudaStream_t s) {
+const uint32_t* launch_slot_of(const StepParams& P, const IdMap& M, int live, int n_ids, cudaStream_t s) {
   if (P.n == 0) return M.slot_of;
+  // after a compaction some upload positions have no slot: their flags stay 0
+  if (n_ids > P.n) cudaMemsetAsync(M.live, 0, sizeof(uint32_t) * (size_t)n_ids, s);
   k_slot_of<<<grid_for(P.n, 256), 256, 0, s>>>(P, M.slot_of, M.live);
-  if (live == P.n) return M.slot_of;  // no removed particle: the ids are the upload positions
-  launch_exclusive_scan(nullptr, M.live, M.pos, (uint32_t)P.n, M.part, nullptr, s);
-  k_compact_ids<<<grid_for(P.n, 256), 256, 0, s>>>(P.n, M.slot_of, M.live, M.pos, M.slot_of_id);
+  if (live == n_ids) return M.slot_of;  // nothing removed since the upload: the ids are the upload positions
+  launch_exclusive_scan(nullptr, M.live, M.pos, (uint32_t)n_ids, M.part, nullptr, s);
+  k_compact_ids<<<grid_for(n_ids, 256), 256, 0, s>>>(n_ids, M.slot_of, M.live, M.pos, M.slot_of_id);
   return M.slot_of_id;
 }
 

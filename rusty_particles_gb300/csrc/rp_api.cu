@@ -232,11 +232,7 @@ int rp_add_particles(rp_sim* s, size_t n, const double* xyz, const double* radiu
     set_error("rp_add_particles: null array");
     return RP_E_INVALID_ARG;
   }
-  for (size_t i = 0; i < n; ++i) {
-    int r = s->e->add_particle(xyz + 3 * i, radius[i], mass[i], fixed ? fixed[i] : 0);
-    if (r != RP_OK) return r;
-  }
-  return RP_OK;
+  return s->e->add_particles(n, xyz, radius, mass, fixed);
 }
 
 int rp_add_mesh_stl(rp_sim* s, const char* path) {

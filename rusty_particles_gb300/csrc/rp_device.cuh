@@ -155,6 +155,7 @@ struct StepParams {
   // reference grid (parity-mode visit rule)
   double href, inv_href;
   int rdims[3];
+  int same_cell_visits;  // ref_visits(c, c) for a cell c inside the grid (3 per periodic axis of one cell, else 1)
   // fine grid (neighbour search)
   double fmin[3], fcell[3];
   int fdims[3];
@@ -281,6 +282,17 @@ __device__ __forceinline__ int ref_visits(const StepParams& P, unsigned long lon
     if (m == 0) return 0;
   }
   return m;
+}
+
+// Whether a reference-cell code lies inside the grid (the reference inserted
+// the particle, src/grid.rs:34-37).
+__device__ __forceinline__ bool ref_inside(const StepParams& P, unsigned long long c) {
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const int32_t b = code_axis(c, k);
+    if (b < 0 || b >= P.rdims[k]) return false;
+  }
+  return true;
 }
 
 // Fine-grid cell of a position: periodic axes wrap, open axes clamp.

@@ -68,7 +68,8 @@ struct StateIO {
 struct IdMap {
   uint32_t *slot_of, *live, *pos, *slot_of_id, *part;
 };
-const uint32_t* launch_slot_of(const StepParams& P, const IdMap& M, int live, cudaStream_t s);
+// n_ids: upload positions (the tags range over [0, n_ids)); live: particles alive.
+const uint32_t* launch_slot_of(const StepParams& P, const IdMap& M, int live, int n_ids, cudaStream_t s);
 void launch_state_gather(const StepParams& P, const uint32_t* slot_of, const StateIO& io, int m, cudaStream_t s);
 void launch_state_same(const StepParams& P, const uint32_t* slot_of, const StateIO& io, unsigned* differs, int m,
                        cudaStream_t s);

@@ -237,6 +237,63 @@ def test_mixed_precision_one_step(rp, oracle_mod, normal):
     assert float(et.max(initial=0)) <= 1e-5, float(et.max())
 
 
+def _mixed_vs_oracle(rp, oracle_mod, st, lo, hi, tangential, dt=1e-6):
+    o = pu.oracle_sim(oracle_mod, st, dt, lo, hi, 1, tangential)
+    g = pu.gpu_sim(rp, st, dt, lo, hi, 1, tangential, precision=1)
+    o.step()
+    g.step()
+    Fo, To = o.last_forces()
+    Fg, Tg = g.debug_forces()
+    FS, TS = o.last_force_scale()
+    m = FS > 0
+    assert np.count_nonzero(m) > 100
+    ef = np.linalg.norm(Fg - Fo, axis=1)[m] / FS[m]
+    et = np.linalg.norm(Tg - To, axis=1)[m] / np.maximum(TS[m], 1e-300)
+    return float(ef.max()), float(et.max())
+
+
+def test_mixed_precision_spinning_grazing_contacts(rp, oracle_mod):
+    # fast spins (|w r| ~ 3 m/s) on contacts overlapping by 1e-7 m: the
+    # normal relative speed (damping) is small next to the spin terms, whose
+    # rounding must not reach it (the spin adds nothing along the normal)
+    k = 12
+    r = 0.01
+    g3 = np.stack(np.meshgrid(*[np.arange(k)] * 3, indexing="ij"), -1).reshape(-1, 3)
+    x = -0.15 + g3 * (2 * r - 1e-7)
+    n = len(x)
+    rng = np.random.default_rng(3)
+    st = {"position": x, "radius": np.full(n, r), "mass": np.full(n, 2500.0 * 4.0 / 3.0 * np.pi * r ** 3),
+          "velocity": rng.normal(0, 1e-4, (n, 3)), "angular_velocity": rng.normal(0, 300.0, (n, 3)),
+          "acceleration": np.zeros((n, 3)), "torque": np.zeros((n, 3)), "fixed": np.zeros(n, np.uint8)}
+    ef, et = _mixed_vs_oracle(rp, oracle_mod, st, (-0.3, -0.3, -0.3), (0.3, 0.3, 0.3), 2)
+    assert ef <= 1e-5, ef
+
+
+def test_mixed_precision_rolling_pairs_friction(rp, oracle_mod):
+    # pairs rolling against each other with a slip of 1 mm/s under spins of
+    # 300 rad/s: the friction direction is the slip's, a small difference of
+    # the velocity and spin terms
+    r = 0.01
+    pairs = 400
+    c = np.stack(np.meshgrid(np.arange(20), np.arange(20), indexing="ij"), -1).reshape(-1, 2) * 0.05 - 0.475
+    x = np.zeros((2 * pairs, 3))
+    x[0::2, 0], x[0::2, 2] = c[:, 0] + r - 2e-6, c[:, 1]
+    x[1::2, 0], x[1::2, 2] = c[:, 0] - r + 2e-6, c[:, 1]
+    n = len(x)
+    w = np.zeros((n, 3))
+    w[:, 2] = 300.0
+    v = np.zeros((n, 3))
+    # i even, j odd, normal from j to i = +x: the contact points move with
+    # v_i - 300 r y and v_j + 300 r y, so the slip is (v_i - v_j)_y - 6 m/s
+    v[0::2, 1] = 3.0 + 0.5e-3
+    v[1::2, 1] = -3.0 - 0.5e-3
+    st = {"position": x, "radius": np.full(n, r), "mass": np.full(n, 2500.0 * 4.0 / 3.0 * np.pi * r ** 3),
+          "velocity": v, "angular_velocity": w, "acceleration": np.zeros((n, 3)), "torque": np.zeros((n, 3)),
+          "fixed": np.zeros(n, np.uint8)}
+    ef, et = _mixed_vs_oracle(rp, oracle_mod, st, (-0.6, -0.6, -0.6), (0.6, 0.6, 0.6), 0)
+    assert ef <= 1e-5 and et <= 1e-5, (ef, et)
+
+
 def test_many_steps_stay_close(rp, oracle_mod):
     # Hertz with the reference's Mindlin (zero tangential force) on a touching
     # bed: 200 steps stay within rounding of the oracle. With Coulomb friction
@@ -309,6 +366,44 @@ def test_removal_and_reindex(rp, oracle_mod):
     so, sg = o.state(), g.get_state()
     np.testing.assert_array_equal(sg["radius"], so["r"])
     assert np.max(np.abs(sg["position"] - so["x"])) < 1e-12
+    # the removed particles left the slots on the device: one upload (the
+    # first step), no download, a compaction after the steps that removed
+    s = g.stats()
+    assert s["state_uploads"] == 1 and s["state_downloads"] == 0 and s["compactions"] >= 1, s
+    for _ in range(3):  # and stepping on from the compacted slots still matches
+        o.step()
+        g.step()
+    so, sg = o.state(), g.get_state()
+    assert g.get_particle_count() == o.get_particle_count()
+    assert np.max(np.abs(sg["position"] - so["x"])) < 1e-12
+    assert g.stats()["state_uploads"] == 1
+
+
+def test_insertion_on_the_device(rp, oracle_mod):
+    # particles added between steps (src/simulation.rs:93-96) go to the end of
+    # the ids; while the device holds the state they are appended to its slots
+    lo, hi = (-0.2, -0.2, -0.2), (0.2, 0.2, 0.2)
+    st = pu.random_bed(52, 500, lo, hi, 0.008, 0.012)
+    st["velocity"][::9] = np.array([0.0, -800.0, 0.0])  # these leave the box in the steps after the insertion
+    o, g = one_step(rp, oracle_mod, st, 1, 0, lo, hi, dt=1e-3)
+    g.step()
+    o.step()
+    rng = np.random.default_rng(9)
+    x = rng.uniform(-0.15, 0.15, (20, 3))
+    r = rng.uniform(0.008, 0.012, 20)
+    m = 2500.0 * 4.0 / 3.0 * np.pi * r ** 3
+    g.add_particles(x, r, m)
+    for i in range(20):
+        o.add_particle(x[i, 0], x[i, 1], x[i, 2], r[i], m[i])
+    for _ in range(3):
+        o.step()
+        g.step()
+    assert g.get_particle_count() == o.get_particle_count()
+    so, sg = o.state(), g.get_state()
+    np.testing.assert_array_equal(sg["radius"], so["r"])
+    assert np.max(np.abs(sg["position"] - so["x"])) < 1e-12
+    s = g.stats()
+    assert s["device_inserts"] == 20 and s["state_uploads"] == 1 and s["state_downloads"] == 0, s
 
 
 def test_neighbour_list_growth(rp, oracle_mod):
