@@ -212,6 +212,15 @@ int rp_debug_contact_pairs(rp_sim* sim, int64_t* pi, int64_t* pj, int32_t* visit
  * (the flattened `cells` vectors); *n_order = number of inserted particles. */
 int rp_debug_reference_grid(rp_sim* sim, double h, int64_t* cell_of, int64_t* order, size_t* n_order,
                             int32_t dims[3]);
+/* The triangle grid of the wall contacts as built on the device (replaces the
+ * every-triangle loop of src/simulation.rs:464-523 with the triangles of the
+ * centre's cell, in mesh order): dims, lo_cell = {origin x, y, z, cell size},
+ * start[c] (ncells + 1 entries; *n_start receives ncells + 1) and the triangle
+ * ids of cell c at items[start[c] .. start[c+1]) (*n_items receives their
+ * count). Arrays shorter than needed are left untouched (query with NULL).
+ * Uploads the state first when the device does not hold it. */
+int rp_debug_triangle_grid(rp_sim* sim, int32_t dims[3], double lo_cell[4], uint32_t* start, size_t start_cap,
+                           uint32_t* items, size_t items_cap, size_t* n_start, size_t* n_items);
 
 /* --- groups: independent beds stepped together (no counterpart in the
  * reference, which simulates one bed per Simulation). A group is what one

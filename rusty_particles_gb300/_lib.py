@@ -166,6 +166,9 @@ SIGNATURES = {
     "rp_debug_last_forces": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp]),
     "rp_debug_contact_pairs": (ctypes.c_int, [ctypes.c_void_p, _i64p, _i64p, _i32p, ctypes.c_size_t,
                                               ctypes.POINTER(ctypes.c_size_t)]),
+    "rp_debug_triangle_grid": (ctypes.c_int, [ctypes.c_void_p, _i32p, _dp, _u32p, ctypes.c_size_t, _u32p,
+                                              ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t),
+                                              ctypes.POINTER(ctypes.c_size_t)]),
     "rp_debug_reference_grid": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, _i64p, _i64p,
                                                ctypes.POINTER(ctypes.c_size_t), _i32p]),
     "rp_cell_sort_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_size_t, _dp, ctypes.c_double, _i32p,

@@ -22,8 +22,9 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=o
           "-I", CSRC]
 # Per-file extra flags: the step kernels and the JKR sample generator must not
 # fuse multiply-adds (their rounding has to match the oracle's).
-EXTRA = {"k_step.cu": ["-fmad=false"], "k_mlp.cu": ["-fmad=false"]}
-SOURCES = ["k_broadphase.cu", "k_step.cu", "engine.cu", "rp_api.cu", "k_noalloc.cu", "k_mlp.cu", "k_fp64.cu"]
+EXTRA = {"k_step.cu": ["-fmad=false"], "k_mlp.cu": ["-fmad=false"], "k_trigrid.cu": ["-fmad=false"]}
+SOURCES = ["k_broadphase.cu", "k_step.cu", "engine.cu", "rp_api.cu", "k_noalloc.cu", "k_mlp.cu", "k_fp64.cu",
+           "k_trigrid.cu"]
 
 
 def nvcc() -> str:

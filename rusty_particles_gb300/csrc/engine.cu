@@ -69,46 +69,6 @@ Law Engine::make_law(const Material& m) const {
   return L;
 }
 
-// Squared distance from p to the triangle (a, b, c): the closest point by
-// its Voronoi region (Ericson, Real-Time Collision Detection, 2005, 5.1.5).
-static double point_triangle_dist2(const double p[3], const double a[3], const double b[3], const double c[3]) {
-  auto sub = [](const double* u, const double* v, double* w) { for (int k = 0; k < 3; ++k) w[k] = u[k] - v[k]; };
-  auto dot = [](const double* u, const double* v) { return u[0] * v[0] + u[1] * v[1] + u[2] * v[2]; };
-  auto d2to = [&](const double* q) { double w[3]; sub(p, q, w); return dot(w, w); };
-  double ab[3], ac[3], ap[3], bp[3], cp[3], q[3];
-  sub(b, a, ab); sub(c, a, ac); sub(p, a, ap);
-  const double d1 = dot(ab, ap), d2 = dot(ac, ap);
-  if (d1 <= 0.0 && d2 <= 0.0) return dot(ap, ap);
-  sub(p, b, bp);
-  const double d3 = dot(ab, bp), d4 = dot(ac, bp);
-  if (d3 >= 0.0 && d4 <= d3) return dot(bp, bp);
-  const double vc = d1 * d4 - d3 * d2;
-  if (vc <= 0.0 && d1 >= 0.0 && d3 <= 0.0) {
-    const double v = d1 / (d1 - d3);
-    for (int k = 0; k < 3; ++k) q[k] = a[k] + v * ab[k];
-    return d2to(q);
-  }
-  sub(p, c, cp);
-  const double d5 = dot(ab, cp), d6 = dot(ac, cp);
-  if (d6 >= 0.0 && d5 <= d6) return dot(cp, cp);
-  const double vb = d5 * d2 - d1 * d6;
-  if (vb <= 0.0 && d2 >= 0.0 && d6 <= 0.0) {
-    const double w = d2 / (d2 - d6);
-    for (int k = 0; k < 3; ++k) q[k] = a[k] + w * ac[k];
-    return d2to(q);
-  }
-  const double va = d3 * d6 - d5 * d4;
-  if (va <= 0.0 && d4 - d3 >= 0.0 && d5 - d6 >= 0.0) {
-    const double w = (d4 - d3) / ((d4 - d3) + (d5 - d6));
-    for (int k = 0; k < 3; ++k) q[k] = b[k] + w * (c[k] - b[k]);
-    return d2to(q);
-  }
-  const double den = 1.0 / (va + vb + vc);
-  const double v = vb * den, w = vc * den;
-  for (int k = 0; k < 3; ++k) q[k] = a[k] + ab[k] * v + ac[k] * w;
-  return d2to(q);
-}
-
 static int bits_for(uint64_t maxkey) {
   int b = 1;
   while (b < 32 && (1ull << b) <= maxkey) ++b;
@@ -616,10 +576,13 @@ int Engine::build_params() {
 }
 
 // Uniform grid over the triangles: each triangle is listed in every cell its
-// bounding box, grown by the largest particle radius, overlaps; a particle
-// then tests only the triangles of the cell holding its centre. Lists keep
-// triangle (mesh) order, so contributions sum in the reference's order
-// (src/simulation.rs:465-466).
+// bounding box, grown by the largest particle radius, overlaps and whose
+// centre lies within reach of it; a particle then tests only the triangles of
+// the cell holding its centre. Lists keep triangle (mesh) order, so
+// contributions sum in the reference's order (src/simulation.rs:465-466).
+// The host does the O(T) set-up from the mesh it holds (grown boxes, cell
+// size, candidate counts); k_trigrid.cu builds the records and the lists on
+// the device.
 int Engine::build_triangle_grid(double rmax) {
   const size_t T = tri_v_.size() / 9;
   P_.ntri = (int)T;
@@ -630,12 +593,15 @@ int Engine::build_triangle_grid(double rmax) {
     P_.titems = nullptr;
     return RP_OK;
   }
+  if (T > (size_t)0x3FFFFFF) {
+    set_error("too many triangles (%zu)", T);
+    return RP_E_INVALID_ARG;
+  }
   if (!motions_.empty()) {
     TRY(dalloc(&motions_d_, motions_.size()));
     CK(cudaMemcpy(motions_d_, motions_.data(), sizeof(WallMotion) * motions_.size(), cudaMemcpyHostToDevice));
     P_.motions = motions_d_;
   }
-  std::vector<TriRec> recs(T);
   double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
   std::vector<double> blo(3 * T), bhi(3 * T);
   // Cells are looked up in FP32 on the device (error ~1e-7 of the coordinate),
@@ -646,51 +612,7 @@ int Engine::build_triangle_grid(double rmax) {
   const double grow = rmax * (1.0 + 1e-6) + 1e-6 * (1.0 + extent_abs + rmax);
   for (size_t t = 0; t < T; ++t) {
     const float* q = &tri_v_[9 * t];
-    TriRec& r = recs[t];
-    double v0[3] = {q[0], q[1], q[2]}, v1[3] = {q[3], q[4], q[5]}, v2[3] = {q[6], q[7], q[8]};
-    for (int k = 0; k < 3; ++k) {
-      r.v0[k] = v0[k];
-      r.e0[k] = v1[k] - v0[k];
-      r.e1[k] = v2[k] - v0[k];
-      r.n[k] = tri_n_[3 * t + k];
-    }
-    r.a = r.e0[0] * r.e0[0] + r.e0[1] * r.e0[1] + r.e0[2] * r.e0[2];
-    r.b = r.e0[0] * r.e1[0] + r.e0[1] * r.e1[1] + r.e0[2] * r.e1[2];
-    r.c = r.e1[0] * r.e1[0] + r.e1[1] * r.e1[1] + r.e1[2] * r.e1[2];
-    r.det = r.a * r.c - r.b * r.b;
-    r.denom = r.a - 2.0 * r.b + r.c;
-    r.group = t < tri_group_.size() ? tri_group_[t] : GROUP_ALL;
-    r.motion = t < tri_motion_.size() ? tri_motion_[t] : NO_MOTION;
-    {
-      double cx = r.e0[1] * r.e1[2] - r.e0[2] * r.e1[1], cy = r.e0[2] * r.e1[0] - r.e0[0] * r.e1[2],
-             cz = r.e0[0] * r.e1[1] - r.e0[1] * r.e1[0];
-      double l = std::sqrt(cx * cx + cy * cy + cz * cz);
-      for (int e = 0; e < 3; ++e) r.edge[e] = make_float4(0.f, 0.f, 0.f, 1e30f);  // never rejects
-      if (l > 0.0 && std::isfinite(l)) {
-        cx /= l; cy /= l; cz /= l;
-        r.plane = make_float4((float)cx, (float)cy, (float)cz, (float)(cx * v0[0] + cy * v0[1] + cz * v0[2]));
-        // in-plane unit normals of the edges, pointing away from the triangle
-        const double* vv[3] = {v0, v1, v2};
-        for (int e = 0; e < 3; ++e) {
-          const double *p = vv[e], *q2 = vv[(e + 1) % 3], *o = vv[(e + 2) % 3];
-          const double d[3] = {q2[0] - p[0], q2[1] - p[1], q2[2] - p[2]};
-          double m[3] = {d[1] * cz - d[2] * cy, d[2] * cx - d[0] * cz, d[0] * cy - d[1] * cx};
-          const double ml = std::sqrt(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]);
-          if (!(ml > 0.0) || !std::isfinite(ml)) continue;
-          for (int k = 0; k < 3; ++k) m[k] /= ml;
-          if (m[0] * (o[0] - p[0]) + m[1] * (o[1] - p[1]) + m[2] * (o[2] - p[2]) > 0.0)
-            for (int k = 0; k < 3; ++k) m[k] = -m[k];
-          r.edge[e] = make_float4((float)m[0], (float)m[1], (float)m[2],
-                                  (float)(m[0] * p[0] + m[1] * p[1] + m[2] * p[2]));
-        }
-      } else {
-        r.plane = make_float4(0.f, 0.f, 0.f, 0.f);
-      }
-      double vm = 0.0;
-      for (int k = 0; k < 3; ++k)
-        vm = std::max(vm, std::max(std::fabs(v0[k]), std::max(std::fabs(v1[k]), std::fabs(v2[k]))));
-      r.bound = make_float4((float)vm, 0.f, 0.f, 0.f);
-    }
+    const double v0[3] = {q[0], q[1], q[2]}, v1[3] = {q[3], q[4], q[5]}, v2[3] = {q[6], q[7], q[8]};
     for (int k = 0; k < 3; ++k) {
       double mn = std::min(v0[k], std::min(v1[k], v2[k])) - grow;
       double mx = std::max(v0[k], std::max(v1[k], v2[k])) + grow;
@@ -701,12 +623,18 @@ int Engine::build_triangle_grid(double rmax) {
     }
   }
   double ext = std::max(hi[0] - lo[0], std::max(hi[1] - lo[1], hi[2] - lo[2]));
-  // cells of about a radius keep the per-cell lists (pruned by distance below) short
+  // cells of about a radius keep the per-cell lists (pruned by distance) short
   double cell = std::max(rmax, ext / 1024.0);
   if (!(cell > 0.0)) cell = 1.0;
-  std::vector<uint32_t> counts;
-  int dims[3];
-  uint64_t entries = 0;
+  int dims[3] = {1, 1, 1};
+  std::vector<int> box(6 * T);
+  std::vector<uint32_t> coff(T + 1, 0);
+  auto cell_box = [&](size_t t, int a[3], int b[3]) {
+    for (int k = 0; k < 3; ++k) {
+      a[k] = std::max(0, (int)std::floor((blo[3 * t + k] - lo[k]) / cell));
+      b[k] = std::min(dims[k] - 1, (int)std::floor((bhi[3 * t + k] - lo[k]) / cell));
+    }
+  };
   for (int iter = 0; iter < 80; ++iter) {
     uint64_t tot = 1;
     for (int k = 0; k < 3; ++k) {
@@ -717,58 +645,88 @@ int Engine::build_triangle_grid(double rmax) {
       cell *= 1.5;
       continue;
     }
-    entries = 0;
+    uint64_t entries = 0;
     for (size_t t = 0; t < T; ++t) {
-      uint64_t c = 1;
-      for (int k = 0; k < 3; ++k) {
-        int a = std::max(0, (int)std::floor((blo[3 * t + k] - lo[k]) / cell));
-        int b = std::min(dims[k] - 1, (int)std::floor((bhi[3 * t + k] - lo[k]) / cell));
-        c *= (uint64_t)(b - a + 1);
-      }
-      entries += c;
+      int a[3], b[3];
+      cell_box(t, a, b);
+      entries += (uint64_t)(b[0] - a[0] + 1) * (uint64_t)(b[1] - a[1] + 1) * (uint64_t)(b[2] - a[2] + 1);
     }
     if (entries <= 64ull * T + (1ull << 22)) break;
     cell *= 1.5;
   }
-  const size_t nc = (size_t)dims[0] * dims[1] * dims[2];
-  std::vector<uint32_t> start(nc + 1, 0);
-  // A triangle is listed in the cells of its grown box whose centre lies
-  // within half a cell diagonal plus the growth of the triangle itself: a
-  // centre that rounds into such a cell and lies within rmax of the triangle
-  // is within that distance of the cell's centre (degenerate triangles keep
-  // the whole box).
-  const double reach = cell * std::sqrt(3.0) * 0.5 + grow;
-  const double reach2 = reach * reach * (1.0 + 1e-9) + 1e-24;
-  auto for_cells = [&](size_t t, auto&& f) {
+  uint64_t total = 0;
+  for (size_t t = 0; t < T; ++t) {
     int a[3], b[3];
+    cell_box(t, a, b);
     for (int k = 0; k < 3; ++k) {
-      a[k] = std::max(0, (int)std::floor((blo[3 * t + k] - lo[k]) / cell));
-      b[k] = std::min(dims[k] - 1, (int)std::floor((bhi[3 * t + k] - lo[k]) / cell));
+      box[6 * t + k] = a[k];
+      box[6 * t + 3 + k] = b[k];
     }
-    const float* q = &tri_v_[9 * t];
-    const double v0[3] = {q[0], q[1], q[2]}, v1[3] = {q[3], q[4], q[5]}, v2[3] = {q[6], q[7], q[8]};
-    const bool flat = recs[t].plane.x == 0.f && recs[t].plane.y == 0.f && recs[t].plane.z == 0.f;
-    for (int z = a[2]; z <= b[2]; ++z)
-      for (int y = a[1]; y <= b[1]; ++y)
-        for (int x = a[0]; x <= b[0]; ++x) {
-          if (!flat) {
-            const double cc[3] = {lo[0] + (x + 0.5) * cell, lo[1] + (y + 0.5) * cell, lo[2] + (z + 0.5) * cell};
-            if (point_triangle_dist2(cc, v0, v1, v2) > reach2) continue;  // NaN keeps the cell
-          }
-          f((size_t)x + (size_t)dims[0] * ((size_t)y + (size_t)dims[1] * z));
-        }
+    coff[t] = (uint32_t)total;
+    total += (uint64_t)(b[0] - a[0] + 1) * (uint64_t)(b[1] - a[1] + 1) * (uint64_t)(b[2] - a[2] + 1);
+    if (total > 0xFFFFFFF0ull) {
+      set_error("triangle grid too large");
+      return RP_E_INVALID_ARG;
+    }
+  }
+  coff[T] = (uint32_t)total;
+  TriGridShape S;
+  for (int k = 0; k < 3; ++k) {
+    S.lo[k] = lo[k];
+    S.dims[k] = dims[k];
+  }
+  S.cell = cell;
+  S.ncells = (uint32_t)((size_t)dims[0] * dims[1] * dims[2]);
+  // a centre that rounds into a cell and lies within rmax of the triangle is
+  // within half a cell diagonal plus the growth of the cell's centre
+  // (degenerate triangles keep the whole box)
+  const double reach = cell * std::sqrt(3.0) * 0.5 + grow;
+  S.reach2 = reach * reach * (1.0 + 1e-9) + 1e-24;
+  // the mesh and the set-up go to the device; records and lists are built there
+  const size_t nc = S.ncells;
+  const uint32_t n = (uint32_t)total;
+  float *v_d = nullptr, *n_d = nullptr;
+  uint32_t *g_d = nullptr, *m_d = nullptr, *coff_d = nullptr, *ka = nullptr, *va = nullptr, *kb = nullptr,
+           *vb = nullptr, *hist = nullptr, *part = nullptr, *counts = nullptr;
+  int* box_d = nullptr;
+  int rc = RP_OK;
+  auto cleanup = [&]() {
+    dfree(v_d); dfree(n_d); dfree(g_d); dfree(m_d); dfree(coff_d); dfree(box_d);
+    dfree(ka); dfree(va); dfree(kb); dfree(vb); dfree(hist); dfree(part); dfree(counts);
   };
-  for (size_t t = 0; t < T; ++t) for_cells(t, [&](size_t c) { start[c + 1]++; });
-  for (size_t c = 0; c < nc; ++c) start[c + 1] += start[c];
-  std::vector<uint32_t> items(start[nc]);
-  std::vector<uint32_t> fill(start.begin(), start.end() - 1);
-  for (size_t t = 0; t < T; ++t) for_cells(t, [&](size_t c) { items[fill[c]++] = (uint32_t)t; });
-  TRY(dalloc(&tri_d_, T));
-  TRY(dalloc(&tstart_d_, nc + 1));
-  TRY(dalloc(&titems_d_, std::max<size_t>(items.size(), 1)));
-  CK(cudaMemcpy(tri_d_, recs.data(), sizeof(TriRec) * T, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(tstart_d_, start.data(), sizeof(uint32_t) * (nc + 1), cudaMemcpyHostToDevice));
-  if (!items.empty()) CK(cudaMemcpy(titems_d_, items.data(), sizeof(uint32_t) * items.size(), cudaMemcpyHostToDevice));
+  const uint32_t hn = radix_hist_needed(std::max<uint32_t>(n, 1));
+  if ((rc = dalloc(&v_d, 9 * T)) || (rc = dalloc(&n_d, 3 * T)) || (rc = dalloc(&g_d, T)) || (rc = dalloc(&m_d, T)) ||
+      (rc = dalloc(&coff_d, T + 1)) || (rc = dalloc(&box_d, 6 * T)) || (rc = dalloc(&ka, n)) ||
+      (rc = dalloc(&va, n)) || (rc = dalloc(&kb, n)) || (rc = dalloc(&vb, n)) || (rc = dalloc(&hist, hn)) ||
+      (rc = dalloc(&part, scan_parts_needed(std::max<uint32_t>(hn, (uint32_t)nc + 1)) + 16)) ||
+      (rc = dalloc(&counts, nc + 1)) || (rc = dalloc(&tri_d_, T)) || (rc = dalloc(&tstart_d_, nc + 1)) ||
+      (rc = dalloc(&titems_d_, std::max<size_t>(n, 1)))) {
+    cleanup();
+    return rc;
+  }
+  cudaError_t e = cudaMemcpyAsync(v_d, tri_v_.data(), sizeof(float) * 9 * T, cudaMemcpyHostToDevice, stream_);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(n_d, tri_n_.data(), sizeof(float) * 3 * T, cudaMemcpyHostToDevice, stream_);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(g_d, tri_group_.data(), sizeof(uint32_t) * T, cudaMemcpyHostToDevice, stream_);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(m_d, tri_motion_.data(), sizeof(uint32_t) * T, cudaMemcpyHostToDevice, stream_);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(coff_d, coff.data(), sizeof(uint32_t) * (T + 1), cudaMemcpyHostToDevice, stream_);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(box_d, box.data(), sizeof(int) * 6 * T, cudaMemcpyHostToDevice, stream_);
+  const uint32_t* items = nullptr;
+  if (e == cudaSuccess) {
+    launch_triangle_grid(v_d, n_d, g_d, m_d, (int)T, box_d, coff_d, n, S, tri_d_, ka, va, kb, vb, hist, part,
+                         counts, tstart_d_, stream_, &items);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess && n > 0)
+    e = cudaMemcpyAsync(titems_d_, items, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, stream_);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(stream_);
+  cleanup();
+  if (e != cudaSuccess) {
+    set_error("triangle grid build failed: %s", cudaGetErrorString(e));
+    return RP_E_CUDA;
+  }
   P_.tri = tri_d_;
   P_.tstart = tstart_d_;
   P_.titems = titems_d_;
@@ -779,6 +737,36 @@ int Engine::build_triangle_grid(double rmax) {
   }
   P_.tcell = cell;
   P_.tinvf = (float)(1.0 / cell);
+  tgrid_built_ = true;
+  return RP_OK;
+}
+
+// The device-built triangle grid (for tests): dims, origin and cell size,
+// the cell starts (ncells + 1) and the triangle ids in cell order.
+int Engine::debug_triangle_grid(int32_t dims[3], double lo_cell[4], uint32_t* start, size_t start_cap,
+                                uint32_t* items, size_t items_cap, size_t* n_start, size_t* n_items) {
+  TRY(ensure_gpu());
+  if (!dev_valid_) {
+    if (!host_valid_) TRY(download());
+    TRY(upload());
+  }
+  if (P_.ntri == 0) {
+    *n_start = *n_items = 0;
+    return RP_OK;
+  }
+  const size_t nc = (size_t)P_.tdims[0] * P_.tdims[1] * P_.tdims[2];
+  for (int k = 0; k < 3; ++k) {
+    dims[k] = P_.tdims[k];
+    lo_cell[k] = P_.tmin[k];
+  }
+  lo_cell[3] = P_.tcell;
+  *n_start = nc + 1;
+  uint32_t total = 0;
+  CK(cudaMemcpy(&total, tstart_d_ + nc, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+  *n_items = total;
+  if (start && start_cap >= nc + 1) CK(cudaMemcpy(start, tstart_d_, sizeof(uint32_t) * (nc + 1), cudaMemcpyDeviceToHost));
+  if (items && items_cap >= total && total > 0)
+    CK(cudaMemcpy(items, titems_d_, sizeof(uint32_t) * total, cudaMemcpyDeviceToHost));
   return RP_OK;
 }
 

@@ -72,6 +72,9 @@ class Engine {
   int debug_forces(double* F, double* T);
   int debug_pairs(int64_t* pi, int64_t* pj, int32_t* visits, size_t capacity, size_t* n);
   int debug_reference_grid(double h, int64_t* cell_of, int64_t* order, size_t* n_order, int32_t dims[3]);
+  int debug_triangle_grid(int32_t dims[3], double lo_cell[4], uint32_t* start, size_t start_cap, uint32_t* items,
+                          size_t items_cap, size_t* n_start, size_t* n_items);
+  bool tgrid_built_ = false;
   int write_vtk(const char* path);
   // learned JKR (RP_JKR_*)
   int jkr_solver = RP_JKR_NEWTON;

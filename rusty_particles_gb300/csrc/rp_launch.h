@@ -41,6 +41,24 @@ int launch_reference_grid(const StepParams& P, const D4* xr, int n, uint32_t nce
                           uint32_t* ka, uint32_t* va, uint32_t* kb, uint32_t* vb, uint32_t* hist, uint32_t* part,
                           cudaStream_t s);
 
+// k_trigrid.cu: the triangle grid of the wall contacts. The host passes each
+// triangle's cell box (a0 a1 a2 b0 b1 b2, ints) and the exclusive scan of the
+// box sizes (coff, T+1 entries, total = coff[T]); the device writes the
+// triangle records, sorts the kept (cell, triangle) candidates and writes
+// tstart (ncells+1 entries); *items points at the triangle ids in cell order
+// (ka/va/kb/vb/hist/part are sort buffers for `total` keys, counts ncells+1).
+struct TriGridShape {
+  double lo[3];
+  double cell;
+  int dims[3];
+  uint32_t ncells;
+  double reach2;  // a cell whose centre is farther than sqrt(reach2) from a triangle does not list it
+};
+int launch_triangle_grid(const float* v, const float* nrm, const uint32_t* grp, const uint32_t* mot, int T,
+                         const int* box, const uint32_t* coff, uint32_t total, const TriGridShape& S,
+                         TriRec* recs, uint32_t* ka, uint32_t* va, uint32_t* kb, uint32_t* vb, uint32_t* hist,
+                         uint32_t* part, uint32_t* counts, uint32_t* tstart, cudaStream_t s, const uint32_t** items);
+
 // k_step.cu
 int launch_first_half(const StepParams& P, cudaStream_t s);  // each returns kernels launched
 int launch_second_half(const StepParams& P, cudaStream_t s);
