@@ -241,6 +241,24 @@ __device__ __forceinline__ R normal_mag(int model, R overlap, T3<R> n, T3<R> rv,
   }
   return m;
 }
+// The same with the normal relative speed given (vn = rv . n; the FP32 form
+// forms it in FP64). The hysteretic particle-particle law keeps the
+// reference's zero velocity.
+template <typename R>
+__device__ __forceinline__ R normal_mag_vn(int model, R overlap, T3<R> n, R vn, R es, R rs, R ms, R beta_abs,
+                                          R gamma) {
+  switch (model) {
+    case 1: return hertz_mag(overlap, vn, es, rs, ms, beta_abs);
+    case 0: {
+      R kn = es * rs;
+      R gn = R(0.5) * sqrt(ms * kn);
+      return lsd_mag(overlap, vn, kn, gn);
+    }
+    case 2: return lsd_mag(overlap, dot(t3(R(0), R(0), R(0)), n), es * rs, R(0));
+    case 3: return jkr_mag(overlap, es, rs, gamma);
+    default: return sjkr_mag(overlap, vn, es, rs, gamma);
+  }
+}
 // The vector form, f n, as the reference returns it.
 template <typename R>
 __device__ __forceinline__ T3<R> normal_force(int model, R overlap, T3<R> n, T3<R> rv, R es, R rs, R ms, R beta_abs,
@@ -258,10 +276,16 @@ __device__ __forceinline__ T3<R> coulomb_force(R fn, T3<R> rv, T3<R> n, R mu) {
   T3<R> dir = vt * inv;
   return (-mu * fn) * dir;
 }
+// Coulomb from a given tangential relative velocity vt = rv - (rv . n) n.
+template <typename R>
+__device__ __forceinline__ T3<R> coulomb_force_vt(R fn, T3<R> vt, R mu) {
+  const R vt2 = dot(vt, vt);
+  if (vt2 < R(1e-8)) return t3(R(0), R(0), R(0));
+  return (-mu * fn) * (vt * rsqrt(vt2));
+}
 // src/physics.rs:400-434 with the spring `xi` in registers.
 template <typename R>
-__device__ __forceinline__ T3<R> spring_coulomb(R fn, T3<R> rv, T3<R> n, T3<R>& xi, R kt, R mu, R dt) {
-  T3<R> vt = rv - dot(rv, n) * n;
+__device__ __forceinline__ T3<R> spring_coulomb_vt(R fn, T3<R> vt, T3<R>& xi, R kt, R mu, R dt) {
   xi = xi + vt * dt;
   T3<R> trial = (-kt) * xi;
   R tm = len(trial);
@@ -273,6 +297,10 @@ __device__ __forceinline__ T3<R> spring_coulomb(R fn, T3<R> rv, T3<R> n, T3<R>& 
     return ft;
   }
   return trial;
+}
+template <typename R>
+__device__ __forceinline__ T3<R> spring_coulomb(R fn, T3<R> rv, T3<R> n, T3<R>& xi, R kt, R mu, R dt) {
+  return spring_coulomb_vt(fn, rv - dot(rv, n) * n, xi, kt, mu, dt);
 }
 
 // One contact seen from particle i (src/simulation.rs:358-460), for a pair
@@ -298,42 +326,50 @@ __device__ __forceinline__ bool pair_contact(const StepParams& P, const Law& L, 
   constexpr bool F32 = sizeof(R) == sizeof(float);
   R overlap;
   T3<R> n;
-  V nd;  // the unit normal in FP64 (FP32 form: to ~1e-14, for the relative velocity below)
+  V nd;         // the unit normal in FP64 (FP32 form: to ~1e-14, for the relative velocity below)
+  double ovd;   // the overlap in FP64 (FP32 form: to ~1e-14 of r_sum)
   if (sizeof(R) == sizeof(double)) {
     const double dist = sqrt(d2);
     overlap = (R)(rsum - dist);
+    ovd = (double)overlap;
     const double inv = 1.0 / dist;
     const V nd = dist > 1e-6 ? d * inv : vmk(0.0, 1.0, 0.0);
     n = cvt<R>(nd);
   } else {
-    // overlap = (r_sum^2 - d^2) / (r_sum + d): the difference is taken in FP64
-    const float dist = sqrtf((float)d2);
-    overlap = (R)((float)(rsum * rsum - d2) / ((float)rsum + dist));
     bool far_enough;
     if (d2 > 1.001e-12) far_enough = true;
     else if (d2 < 0.999e-12) far_enough = false;
     else far_enough = sqrt(d2) > 1e-6;  // exact FP64 decision near the threshold
     if (far_enough) {
       // 1/|d| from the FP32 reciprocal square root and one FP64 Newton step
-      // (relative error ~1e-14, no FP64 square root or division)
+      // (relative error ~1e-14, no FP64 square root or division); |d| is
+      // d^2 times it. The overlap is then good to ~1e-14 of r_sum: the JKR
+      // contact radius next to its fold and the damping of a grazing contact
+      // are sensitive to it.
       const double r0 = (double)rsqrtf((float)d2);
       const double inv = r0 * (1.5 - (0.5 * d2) * (r0 * r0));
+      ovd = rsum - d2 * inv;
       nd = d * inv;
       n = cvt<R>(nd);
     } else {
+      ovd = rsum - sqrt(d2);
       nd = vmk(0.0, 1.0, 0.0);
       n = t3(R(0), R(1), R(0));
     }
+    overlap = (R)ovd;
   }
   const R rir = (R)ri, rjr = (R)rj;
   if (overlap > R(0.2) * fmin(rir, rjr)) excess = true;
   const T3<R> ra = (-n) * rir;
   const T3<R> rb = n * rjr;
-  T3<R> rv;
+  T3<R> rv, vt;
+  R vn;
   if (sizeof(R) == sizeof(double)) {
     const T3<R> va = cvt<R>(vi) + cross(cvt<R>(wi), ra);
     const T3<R> vb = cvt<R>(vj) + cross(cvt<R>(wj), rb);
     rv = va - vb;
+    vn = dot(rv, n);
+    vt = rv - vn * n;
   } else {
     // In a rolling or sticking contact, and along the normal, the relative
     // velocity at the contact point is a small difference of large terms
@@ -342,8 +378,15 @@ __device__ __forceinline__ bool pair_contact(const StepParams& P, const Law& L, 
     // formed in FP64, as (v_i - v_j) - (w_i r_i + w_j r_j) x n (the same
     // quantity as va - vb with r_a = -n r_i, r_b = n r_j), and only then
     // rounded for the FP32 laws.
+    // Its normal part (the damping's speed) and tangential part (the slip)
+    // are split in FP64 too: in a sliding contact the normal speed is a
+    // small remainder of |rv|, in a head-on one the slip is.
     const V W = wi * ri + wj * rj;
-    rv = cvt<R>((vi - vj) - cross(W, nd));
+    const V rvd = (vi - vj) - cross(W, nd);
+    const double vnd = dot(rvd, nd);
+    rv = cvt<R>(rvd);
+    vn = (R)vnd;
+    vt = cvt<R>(rvd - vnd * nd);
   }
   const R rs = (rir * rjr) / (rir + rjr);
   const R ms = ((R)mi * (R)mj) / ((R)mi + (R)mj);
@@ -352,7 +395,7 @@ __device__ __forceinline__ bool pair_contact(const StepParams& P, const Law& L, 
   if (P.nmodel == 3 && P.jkr_solver != 0 && !newton && L.gamma_pp > 0.0) {
     double fmd = 0.0;
     uint32_t it = 0;
-    jkind = jkr_learned(P, L, (double)overlap, (double)rs, guess, fmd, it);
+    jkind = jkr_learned(P, L, ovd, (double)rs, guess, fmd, it);
     if (jkind != JKR_FALLBACK) fmag = (R)fmd;
     if (tally) {
       tally[jkind == JKR_CONVERGES ? 0 : (jkind == JKR_ZERO ? 1 : (jkind == JKR_WALK ? 5 : 2))] += 1;
@@ -377,10 +420,9 @@ __device__ __forceinline__ bool pair_contact(const StepParams& P, const Law& L, 
     fmag = jkr_mag<R>(overlap, (R)L.es_pp, rs, (R)L.gamma_pp, &near);
     if (near) return false;
   } else {
-    fmag = normal_mag<R>(P.nmodel, overlap, n, rv, (R)L.es_pp, rs, ms, (R)L.beta_abs, (R)L.gamma_pp, false);
+    fmag = normal_mag_vn<R>(P.nmodel, overlap, n, vn, (R)L.es_pp, rs, ms, (R)L.beta_abs, (R)L.gamma_pp);
   }
   if (F32 && P.nmodel == 4 && L.gamma_pp > 0.0) {
-    const R vn = dot(rv, n);
     const R gamma = (R)L.gamma_pp, es = (R)L.es_pp;
     const R f_pull = R(1.5) * R(kPi) * gamma * rs;
     const R delta_c = -sqrt(R(3) * (R(kPi) * R(kPi)) * (gamma * gamma) * rs / (es * es));
@@ -395,11 +437,12 @@ __device__ __forceinline__ bool pair_contact(const StepParams& P, const Law& L, 
   bool ft_zero = false;  // ft is +0: F = fn + 0 without the additions
   if (P.tmodel == 0) {
     if (F32) {
-      const T3<R> vt = rv - dot(rv, n) * n;
       const R vt2 = dot(vt, vt);
-      if (fabs(vt2 - R(1e-8)) <= R(1e-5) * (dot(rv, rv) + R(1e-8))) return false;
+      if (fabs(vt2 - R(1e-8)) <= R(1e-5) * (vt2 + R(1e-8))) return false;
+      ft = coulomb_force_vt<R>(fnm, vt, (R)L.mu);
+    } else {
+      ft = coulomb_force<R>(fnm, rv, n, (R)L.mu);
     }
-    ft = coulomb_force<R>(fnm, rv, n, (R)L.mu);
   } else if (!PHYS) {
     // G* = 0 in parity mode (src/material.rs:39-50): the spring force is
     // 0 * (...), +-0, or NaN when Mindlin's sqrt(R* delta) is NaN or infinite
@@ -422,7 +465,8 @@ __device__ __forceinline__ bool pair_contact(const StepParams& P, const Law& L, 
       R kt = P.tmodel == 2 ? R(8) * (R)L.gs_pp * sqrt(rs * overlap) : (R)L.gs_pp * rs;
       if (HIST) xi_s = t3((R)hist[0], (R)hist[plane], (R)hist[2 * plane]);
       xi_s = xi_s - dot(xi_s, n) * n;
-      ft = spring_coulomb<R>(fnm, rv, n, xi_s, kt, (R)L.mu, (R)P.dt);
+      ft = F32 ? spring_coulomb_vt<R>(fnm, vt, xi_s, kt, (R)L.mu, (R)P.dt)
+               : spring_coulomb<R>(fnm, rv, n, xi_s, kt, (R)L.mu, (R)P.dt);
     } else {
       ft = t3(R(0), R(0), R(0));
     }
@@ -1392,22 +1436,46 @@ __device__ __forceinline__ void finish_particle(const StepParams& P, const Bank&
   B.tq[k] = D4{plus_zero(T.x), plus_zero(T.y), plus_zero(T.z), 0.0};
 }
 
-__global__ void __launch_bounds__(256) k_accumulate(StepParams P) {
+// One block per tile of ACC_TILE slots (the tiles k_accum_order sorts
+// within): the tile's contact results are contiguous in cres (offsets are the
+// scan of the per-slot counts in slot order), so the block stages them in
+// shared memory with coalesced loads, ACC_WIN records per round, and each
+// thread sums its own slot's records from there in list order (the same sums
+// as reading them one by one). Threads take the tile's slots in the order
+// aorder gives (similar list lengths per warp).
+constexpr uint32_t ACC_WIN = 1024;  // 48 KB of FP64 results per round
+
+__global__ void __launch_bounds__(ACC_TILE) k_accumulate(StepParams P) {
   Ctrl* C = P.ctrl;
   if (C->halt) return;
   const Bank B = P.bank[C->bank];
   const int lane = threadIdx.x & 31;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n; i += gridDim.x * blockDim.x) {
-    const int k = (int)P.aorder[i];
-    if (B.flags[k] & PF_DEAD) continue;
-    V F = vmk(0.0, 0.0, 0.0), T = vmk(0.0, 0.0, 0.0);
-    const uint32_t n = P.ccnt[k];
-    const double2* res = reinterpret_cast<const double2*>(P.cres + 6 * (size_t)P.coff[k]);
-    for (uint32_t c = 0; c < n; ++c) {
-      const double2 r0 = res[3 * c], r1 = res[3 * c + 1], r2 = res[3 * c + 2];
-      F = F + vmk(r0.x, r0.y, r1.x);
-      T = T + vmk(r1.y, r2.x, r2.y);
+  __shared__ double2 srec[3 * ACC_WIN];
+  for (int base = blockIdx.x * (int)ACC_TILE; base < P.n; base += gridDim.x * (int)ACC_TILE) {
+    const int i = base + (int)threadIdx.x;
+    const int last = min(base + (int)ACC_TILE, P.n) - 1;
+    const uint32_t R0 = P.coff[base], R1 = P.coff[last] + P.ccnt[last];
+    const int k = i < P.n ? (int)P.aorder[i] : -1;
+    uint32_t r0 = 0, r1 = 0;
+    if (k >= 0) {
+      r0 = P.coff[k];
+      r1 = r0 + P.ccnt[k];
     }
+    V F = vmk(0.0, 0.0, 0.0), T = vmk(0.0, 0.0, 0.0);
+    const double2* src = reinterpret_cast<const double2*>(P.cres);
+    for (uint32_t w0 = R0; w0 < R1; w0 += ACC_WIN) {
+      const uint32_t w1 = min(w0 + ACC_WIN, R1);
+      __syncthreads();  // the previous round is consumed
+      for (uint32_t q = threadIdx.x; q < 3 * (w1 - w0); q += ACC_TILE) srec[q] = src[3 * (size_t)w0 + q];
+      __syncthreads();
+      const uint32_t a = max(r0, w0), b = min(r1, w1);
+      for (uint32_t c = a; c < b; ++c) {
+        const double2 x0 = srec[3 * (c - w0)], x1 = srec[3 * (c - w0) + 1], x2 = srec[3 * (c - w0) + 2];
+        F = F + vmk(x0.x, x0.y, x1.x);
+        T = T + vmk(x1.y, x2.x, x2.y);
+      }
+    }
+    if (k < 0 || (B.flags[k] & PF_DEAD)) continue;
     // wall pretests: the first WALL_CAND_CAP triangles that pass are kept
     // for k_accumulate_walls (a count above the cap says there are more)
     uint32_t nc = 0;
@@ -1648,7 +1716,8 @@ static int launch_contact_path(const StepParams& P, cudaStream_t s) {
     else k_contact_deferred<true, false, double><<<P.nsm * 8, 128, 0, s>>>(P);
     ++launched;
   }
-  k_accumulate<<<shaped_grid((uint64_t)P.n, ba, cap), ba, 0, s>>>(P);
+  (void)ba;  // one block per tile of ACC_TILE slots
+  k_accumulate<<<shaped_grid((uint64_t)P.n, ACC_TILE, cap), ACC_TILE, 0, s>>>(P);
   if (P.ntri > 0) {  // over the queue k_accumulate filled; its length is only known on the device
     k_accumulate_walls<<<shaped_grid((uint64_t)P.n, 128, P.nsm * 16), 128, 0, s>>>(P);
     ++launched;

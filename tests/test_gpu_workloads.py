@@ -133,7 +133,9 @@ def test_adhesive_slice(rp, oracle_mod, adhesive, solver, precision, tol):
     assert np.all(np.std(st["velocity"], axis=0) > 0.01)  # a gas, not a settled bed
     o, g = one_step(rp, oracle_mod, wl, st, precision=precision, jkr={"solver": solver, "network": net},
                     cell=bench.max_cutoff(wl), cull=True)
-    check(o, g, tol)
+    # the mixed form's integrator does not carry the Kahan residuals of the
+    # settled state: its positions differ from the oracle's in the last bits
+    check(o, g, tol, exact_positions=precision == "fp64")
     if solver != "newton":
         c = g.jkr_counters()
         assert c["accepted"] > 0 and c["zero"] > 0, c
