@@ -542,20 +542,27 @@ def profiled_traffic(workload_name, n):
         return None, None
 
 
-def fp64_roofline(rp, wl, n, ms_per_step):
-    """The step against the FP64 pipe: the device's FP64 rate measured now by
-    librp (rp_measure_fp64_peak), the FP64-pipe thread instructions per
-    particle-step counted by ncu on a smaller bed of the same workload
-    (profiles/fp64_ops_<workload>.json), and the fraction of that rate the
-    timed step reaches."""
+_FP64_PEAK = {}
+
+
+def fp64_roofline(rp, wl, n, ms_per_step, suffix=""):
+    """The step against the FP64 pipe: the device's FP64 rate measured by
+    librp (rp_measure_fp64_peak, once per run), the FP64-pipe thread
+    instructions per particle-step counted by ncu on a smaller bed of the same
+    workload and form (profiles/fp64_ops_<workload><suffix>.json), and the
+    fraction of that rate the timed step reaches."""
     import ctypes
     from rusty_particles_gb300 import _lib
-    fma, add = ctypes.c_double(), ctypes.c_double()
-    if _lib.load().rp_measure_fp64_peak(ctypes.byref(fma), ctypes.byref(add)) != 0:
-        return None
-    out = {"peak_fma_per_s": fma.value, "peak_add_per_s": add.value, "unit": "FP64 thread instructions/s",
+    if not _FP64_PEAK:
+        fma, add = ctypes.c_double(), ctypes.c_double()
+        if _lib.load().rp_measure_fp64_peak(ctypes.byref(fma), ctypes.byref(add)) != 0:
+            return None
+        _FP64_PEAK.update(fma=fma.value, add=add.value)
+    fma = ctypes.c_double(_FP64_PEAK["fma"])
+    out = {"peak_fma_per_s": _FP64_PEAK["fma"], "peak_add_per_s": _FP64_PEAK["add"],
+           "unit": "FP64 thread instructions/s",
            "peak_source": "measured in this run (librp rp_measure_fp64_peak, CUDA events)"}
-    p = os.path.join(ROOT, "profiles", f"fp64_ops_{wl['name']}.json")
+    p = os.path.join(ROOT, "profiles", f"fp64_ops_{wl['name']}{suffix}.json")
     try:
         with open(p) as f:
             d = json.load(f)
@@ -954,8 +961,9 @@ def run_forms(rp, args, dist, device, log, headline_state, hopper_wl, cache, thr
     def hopper_forms():
         h = forms.setdefault("hopper-1M", {})
         _, r, st = run_form(rp, hopper_wl, args, dist, device, log, precision="mixed", state=headline_state)
+        fp = fp64_roofline(rp, hopper_wl, r["particles"], r["ms_per_step"], "-mixed")
         h["mixed"] = form_entry(r, force_error(rp, hopper_wl, headline_state, "parity", "mixed", None, cache, log,
-                                               threads))
+                                               threads), {"fp64_frac": fp.get("frac") if fp else None})
         _, r, st = run_form(rp, hopper_wl, args, dist, device, log, mode="physical", state=headline_state, settle=300)
         h["physical"] = form_entry(r, force_error(rp, hopper_wl, st, "physical", "fp64", None, cache, log, threads),
                                    {"note": "300 untimed steps from the settled parity state load the springs"})
@@ -1166,7 +1174,8 @@ def run_ours(args, log):
     if ws == 1 and not args.no_forms and args.workload == "hopper" and args.mode == "parity" \
             and args.precision == "fp64":
         got = run_forms(rp, args, dist, local, log, final, wl, cache, threads, t_start + args.forms_budget)
-        forms = {"hopper-1M": {"plain": form_entry(res, ferr), **got.pop("hopper-1M", {})}}
+        plain = form_entry(res, ferr, {"fp64_frac": (res["roofline"].get("fp64") or {}).get("frac")})
+        forms = {"hopper-1M": {"plain": plain, **got.pop("hopper-1M", {})}}
         forms.update(got)
     line = {
         "metric": METRIC, "value": res["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,

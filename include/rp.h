@@ -183,6 +183,14 @@ int rp_set_threads(int n);                               /* set_num_threads (src
 
 /* --- metrics and errors */
 int rp_get_stats(rp_sim* sim, rp_stats* out);
+/* Statistics of the bed in its current state, in FP64 on the device (no
+ * reference counterpart; the reference's scripts compute them in Python):
+ * out[0] kinetic energy, translational plus rotational with I = 2/5 m r^2;
+ * out[1] coordination number, 2 x (pairs with |d| < r_i + r_j, minimum image
+ * on periodic axes) / particles; out[2] solid fraction of the simulation box,
+ * the spheres' summed volume over the box volume. Needs one completed step
+ * (the pair count runs over the neighbour lists). */
+int rp_bed_statistics(rp_sim* sim, double out[3]);
 /* Time every force-kernel launch with CUDA events (adds two event records per step). */
 int rp_set_profiling(rp_sim* sim, int enable);
 const char* rp_last_error(void);

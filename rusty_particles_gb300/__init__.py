@@ -249,6 +249,14 @@ class Simulation:
         check(self._L.rp_get_stats(self._h, ctypes.byref(s)))
         return {k: getattr(s, k) for k, _ in RpStats._fields_}
 
+    def bed_statistics(self):
+        """Kinetic energy, coordination number (2 x overlapping pairs / N) and
+        solid fraction of the box of the current state, computed on the GPU
+        (needs one completed step)."""
+        out = (ctypes.c_double * 3)()
+        check(self._L.rp_bed_statistics(self._h, out))
+        return {"kinetic_energy": out[0], "coordination_number": out[1], "solid_fraction_box": out[2]}
+
     def get_state(self, out=None):
         """All per-particle state as numpy arrays in id order. `out` (a dict as
         returned here, e.g. from an earlier call) is filled in place instead of

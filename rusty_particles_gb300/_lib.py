@@ -158,6 +158,7 @@ SIGNATURES = {
     "rp_set_force_path": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "rp_set_threads": (ctypes.c_int, [ctypes.c_int]),
     "rp_get_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(RpStats)]),
+    "rp_bed_statistics": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]),
     "rp_measure_fp64_peak": (ctypes.c_int, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     "rp_set_profiling": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "rp_last_error": (ctypes.c_char_p, []),

@@ -1499,6 +1499,38 @@ int Engine::stats(rp_stats* s) {
   return RP_OK;
 }
 
+// Bed statistics of the current state (the reference's scripts and SURVEY's
+// long-run checks use these three): kinetic energy, coordination number (2 x
+// overlapping pairs / particles) and the spheres' volume over the box's.
+int Engine::bed_statistics(double out[3]) {
+  TRY(ensure_gpu());
+  if (!dev_valid_ || last_.steps_done == 0) {
+    set_error("step at least once before asking for bed statistics (the count runs over the neighbour lists)");
+    return RP_E_INVALID_ARG;
+  }
+  CK(cudaSetDevice(device_));
+  TRY(sync_ctrl());
+  double* d = nullptr;
+  TRY(dalloc(&d, 3));
+  launch_bed_stats(P_, d, reinterpret_cast<unsigned long long*>(d + 2), stream_);
+  double h[3] = {0.0, 0.0, 0.0};
+  cudaError_t e = cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, stream_);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(stream_);
+  dfree(d);
+  if (e != cudaSuccess) {
+    set_error("bed statistics failed: %s", cudaGetErrorString(e));
+    return RP_E_CUDA;
+  }
+  unsigned long long pairs = 0;
+  std::memcpy(&pairs, &h[2], sizeof(pairs));
+  const double n = (double)n_ - (double)ctrl_h_->removed;
+  const double vbox = (bmax[0] - bmin[0]) * (bmax[1] - bmin[1]) * (bmax[2] - bmin[2]);
+  out[0] = h[0];
+  out[1] = n > 0.0 ? (double)pairs / n : 0.0;
+  out[2] = vbox > 0.0 ? h[1] / vbox : 0.0;
+  return RP_OK;
+}
+
 // ------------------------------------------------------------ diagnostics
 int Engine::debug_forces(double* F, double* T) {
   if (!gpu_ || !debug) {

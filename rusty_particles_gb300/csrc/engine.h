@@ -69,6 +69,7 @@ class Engine {
   int read_state(rp_state* st);
   int write_state(const rp_state* st);
   int stats(rp_stats* st);
+  int bed_statistics(double out[3]);
   int debug_forces(double* F, double* T);
   int debug_pairs(int64_t* pi, int64_t* pj, int32_t* visits, size_t capacity, size_t* n);
   int debug_reference_grid(double h, int64_t* cell_of, int64_t* order, size_t* n_order, int32_t dims[3]);

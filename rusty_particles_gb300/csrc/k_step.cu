@@ -1646,6 +1646,49 @@ __global__ void k_kinetic(StepParams P, double* out) {
   if ((threadIdx.x & 31) == 0) atomicAdd(out, e);
 }
 
+// Bed statistics of the live slots: out[0] kinetic energy (translational and
+// rotational, I = 2/5 m r^2), out[1] the summed sphere volumes, *pairs the
+// overlapping pairs counted from both ends over the Verlet lists (the exact
+// FP64 test d^2 < (r_i + r_j)^2 on the minimum image; every such pair is in
+// the lists, which hold all pairs within the cutoff plus the skin).
+__global__ void k_bed_stats(StepParams P, double* out, unsigned long long* pairs) {
+  const Bank B = P.bank[P.ctrl->bank];
+  double e = 0.0, vol = 0.0;
+  unsigned long long cnt = 0;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < P.n; k += gridDim.x * blockDim.x) {
+    if (B.flags[k] & PF_DEAD) continue;
+    const D4 v = B.vm[k], w = B.wc[k], x = B.xr[k];
+    const double I = 0.4 * v.w * x.w * x.w;
+    e += 0.5 * v.w * (v.x * v.x + v.y * v.y + v.z * v.z) + 0.5 * I * (w.x * w.x + w.y * w.y + w.z * w.z);
+    vol += (4.0 / 3.0) * kPi * x.w * x.w * x.w;
+    const uint32_t* row = B.nbr + (size_t)k * P.cap;
+    const uint32_t c = B.ncnt[k];
+    for (uint32_t m = 0; m < c; ++m) {
+      const D4 y = B.xr[row[m]];
+      const V d = mic(P, xyz(x) - xyz(y));
+      const double rs = x.w + y.w;
+      if (dot(d, d) < rs * rs) ++cnt;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    e += __shfl_down_sync(0xFFFFFFFFu, e, o);
+    vol += __shfl_down_sync(0xFFFFFFFFu, vol, o);
+    cnt += __shfl_down_sync(0xFFFFFFFFu, cnt, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(&out[0], e);
+    atomicAdd(&out[1], vol);
+    atomicAdd(pairs, cnt);
+  }
+}
+
+void launch_bed_stats(const StepParams& P, double* out, unsigned long long* pairs, cudaStream_t s) {
+  cudaMemsetAsync(out, 0, 2 * sizeof(double), s);
+  cudaMemsetAsync(pairs, 0, sizeof(unsigned long long), s);
+  if (P.n == 0) return;
+  k_bed_stats<<<grid_for(P.n, 256), 256, 0, s>>>(P, out, pairs);
+}
+
 int launch_first_half(const StepParams& P, cudaStream_t s) {
   if (P.n == 0) return 0;
   if (P.prec == 1) k_first_half<false><<<grid_for(P.n, 256), 256, 0, s>>>(P);

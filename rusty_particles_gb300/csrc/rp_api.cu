@@ -616,6 +616,15 @@ int rp_debug_reference_grid(rp_sim* s, double h, int64_t* cell_of, int64_t* orde
   return s->e->debug_reference_grid(h, cell_of, order, n_order, dims);
 }
 
+int rp_bed_statistics(rp_sim* s, double out[3]) {
+  SIM_OR_FAIL(s);
+  if (!out) {
+    set_error("null output");
+    return RP_E_INVALID_ARG;
+  }
+  return s->e->bed_statistics(out);
+}
+
 int rp_debug_triangle_grid(rp_sim* s, int32_t dims[3], double lo_cell[4], uint32_t* start, size_t start_cap,
                            uint32_t* items, size_t items_cap, size_t* n_start, size_t* n_items) {
   SIM_OR_FAIL(s);

@@ -69,6 +69,9 @@ int launch_accum_order(const StepParams& P, cudaStream_t s);  // inside the rebu
 int launch_end_step(const StepParams& P, cudaStream_t s);
 // Kinetic energy (translational + rotational) of the live slots, FP64.
 void launch_kinetic_energy(const StepParams& P, double* out, cudaStream_t s);
+// Bed statistics: out[0] kinetic energy, out[1] summed sphere volumes (both
+// FP64), *pairs overlapping pairs counted from both ends (needs current lists).
+void launch_bed_stats(const StepParams& P, double* out, unsigned long long* pairs, cudaStream_t s);
 
 // Bulk state transfer in id order (ids of the live particles): the eight vector arrays of
 // rp_state in the order position, velocity, angular velocity, acceleration,

@@ -522,3 +522,25 @@ def test_state_transfer_after_removals(rp, oracle_mod):
     for i in (0, 1, n // 2, n - 1):  # per-particle getters read through the host
         assert g.get_particle_velocity(i) == tuple(v[i])
         assert g.get_particle_position(i) == tuple(s["position"][i])
+
+
+def test_bed_statistics(rp):
+    # kinetic energy, coordination number and solid fraction of the current
+    # state, on the GPU, against the same quantities from the state in numpy
+    from scipy.spatial import cKDTree
+    lo, hi = (-0.25, -0.25, -0.25), (0.25, 0.25, 0.25)
+    st = pu.random_bed(81, 3000, lo, hi, 0.008, 0.012)
+    g = pu.gpu_sim(rp, st, 1e-5, lo, hi, 1, 0)
+    g.steps(3)
+    b = g.bed_statistics()
+    s = g.get_state()
+    x, v, w, r, m = s["position"], s["velocity"], s["angular_velocity"], s["radius"], s["mass"]
+    ke = float((0.5 * m * (v * v).sum(1)).sum() + (0.5 * (0.4 * m * r * r) * (w * w).sum(1)).sum())
+    p = cKDTree(x).query_pairs(2.0 * r.max(), output_type="ndarray")
+    d = x[p[:, 0]] - x[p[:, 1]]
+    rs = r[p[:, 0]] + r[p[:, 1]]
+    n_over = int(np.count_nonzero(d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1] + d[:, 2] * d[:, 2] < rs * rs))
+    assert n_over > 1000
+    assert b["coordination_number"] == 2.0 * n_over / len(r)
+    assert b["kinetic_energy"] == pytest.approx(ke, rel=1e-12)
+    assert b["solid_fraction_box"] == pytest.approx(float((4.0 / 3.0 * np.pi * r ** 3).sum()) / 0.5 ** 3, rel=1e-12)
