@@ -875,6 +875,10 @@ def run_form(rp, wl, args, dist, device, log, *, mode="parity", precision="fp64"
                                       "reference_newton": d["fallback"] / ev}
     if tune:
         res["autotune"] = tune
+    try:  # the timed state: kinetic energy, coordination number, solid fraction of the box
+        res["bed"] = sim.bed_statistics()
+    except Exception:  # noqa: BLE001 - a statistic must not cost the measurement
+        res["bed"] = None
     res["roofline"] = roofline_of(sim, wl, n_now, prof_steps or min(steps, 200))
     res["e2e"] = e2e_of(sim, len(wl["radius"]), steps, dist)
     final = sim.get_state()
@@ -904,7 +908,7 @@ def jkr_network(rp, wl, state, log):
 
 
 def form_entry(res, force_err=None, extra=None):
-    e = {k: res[k] for k in ("value", "ms_per_step", "particles", "mode", "precision", "clocks", "gpu_launches")}
+    e = {k: res[k] for k in ("value", "ms_per_step", "particles", "mode", "precision", "clocks", "gpu_launches", "bed")}
     e["e2e"] = {"value": res["e2e"]["value"], "wall_ms": res["e2e"]["wall_ms"],
                 "h2d_bytes_per_step": res["e2e"]["h2d_bytes_per_step"],
                 "d2h_bytes_per_step": res["e2e"]["d2h_bytes_per_step"]}
@@ -1185,7 +1189,7 @@ def run_ours(args, log):
         "roofline": res["roofline"], "cpu_baseline": cpu, "cpu_baseline_literal": cpu_lit,
         "e2e": res["e2e"], "gpu_launches": res["gpu_launches"], "clocks": res["clocks"],
         "force_err": ferr, "precision": args.precision, "wall_s_timed": res["wall_s_timed"],
-        "stats": res["stats"],
+        "stats": res["stats"], "bed": res.get("bed"),
     }
     if "jkr" in res:
         line["jkr"] = res["jkr"]
