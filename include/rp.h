@@ -259,8 +259,7 @@ int rp_add_mesh_triangles_moving(rp_sim* sim, size_t n_triangles, const float* v
 /* --- launch shapes of the force pass (no counterpart in the reference) */
 typedef struct rp_tune_report {
   int32_t force_path; /* 0 contact-parallel, 1 one thread per particle */
-  int32_t bs_filter, bs_force, bs_accum; /* threads per block (bs_accum is kept for the layout: the
-                                            accumulate kernel always runs 256 threads, one tile each) */
+  int32_t bs_filter, bs_force, bs_accum; /* threads per block */
   int32_t grid_cap;   /* largest grid of the grid-stride loops */
   int32_t candidates; /* configurations timed */
   double default_ms, best_ms; /* median force-pass time, default and chosen shape */

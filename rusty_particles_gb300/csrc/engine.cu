@@ -432,6 +432,7 @@ void Engine::refresh_list_ptrs() {
   P_.crec = crec_;
   P_.clist = clist_;
   P_.cres = cres_;
+  P_.cresf = reinterpret_cast<float*>(cres_);
   P_.ccnt = ccnt_;
   P_.aorder = aorder_;
   P_.wq = wq_;
@@ -1661,10 +1662,9 @@ int Engine::debug_reference_grid(double h, int64_t* cell_of, int64_t* order, siz
 // Chooses the force pass's launch shapes on the current state: the pass only
 // reads the state and rewrites a, tau and its scratch buffers, so it can be
 // timed repeatedly (CUDA events on the engine's stream, median of 5 after 2
-// warm-up passes). Coordinate descent over the filter and pair block sizes
-// (64, 128, 256), the grid cap of their grid-stride loops, then the
-// one-thread-per-particle path (the accumulate kernel's shape is fixed: one
-// block per tile of 256 slots). The control block (counters, flags) is
+// warm-up passes). Coordinate descent over the filter, pair and accumulate
+// block sizes (64, 128, 256), the grid cap of their grid-stride loops, then the
+// one-thread-per-particle path. The control block (counters, flags) is
 // restored afterwards. Needs lists (a step already taken); the physical mode's
 // spring history is rewritten by the pass, so that mode is not tuned.
 int Engine::autotune(rp_tune_report* rep) {
@@ -1718,7 +1718,6 @@ int Engine::autotune(rp_tune_report* rep) {
   const int blocks[3] = {64, 128, 256};
   const int caps[3] = {nsm * 4, nsm * 16, nsm * 64};
   for (int dim = 1; dim <= 4; ++dim) {
-    if (dim == 3) continue;  // the accumulate kernel runs one block per tile of 256 slots
     for (int k = 0; k < 3; ++k) {
       int c[5];
       std::memcpy(c, cfg, sizeof(c));

@@ -529,9 +529,10 @@ __device__ __forceinline__ void second_half_kick(V& v, V& vres, V& w, V& wres, V
 // the reference's Kahan residuals neither read nor updated. From zero
 // residuals one step gives the same bits as the compensated form; over many
 // steps positions and velocities differ from it by FP64 rounding (about one
-// ulp per step), far below the FP32 pair forces' 1e-5. It takes ~60 of the
-// ~85 FP64 operations per particle and 128 of the 484 bytes (the residuals'
-// read and three writes) off this kernel.
+// ulp per step), far below the FP32 pair forces' 1e-5. With the previous
+// step's second half kick pending, the two half kicks are one kick of a dt.
+// It takes ~45 of the ~85 FP64-pipe instructions per particle and 128 of the
+// 484 bytes (the residuals' read and three writes) off this kernel.
 template <bool KAHAN>
 __global__ void __launch_bounds__(256) k_first_half(StepParams P) {
   Ctrl* C = P.ctrl;
@@ -568,16 +569,14 @@ __global__ void __launch_bounds__(256) k_first_half(StepParams P) {
         wres = xyz(wr4);
         xres = xyz(B.xres[k]);
       }
-      dv = a * hdt;
-      dw = (tau * inv_inertia) * hdt;
-      if (FUSE) {
-        if (KAHAN) {
-          kahan_add(v, vres, dv);
-          kahan_add(w, wres, dw);
-        } else {
-          v = v + dv;
-          w = w + dw;
-        }
+      // the mixed form joins the pending second half kick and this step's
+      // first half kick into one kick of a dt
+      const double kdt = (!KAHAN && FUSE) ? dt : hdt;
+      dv = a * kdt;
+      dw = (tau * inv_inertia) * kdt;
+      if (KAHAN && FUSE) {
+        kahan_add(v, vres, dv);
+        kahan_add(w, wres, dw);
       }
     }
     if (anyp) {
@@ -1189,6 +1188,30 @@ __global__ void __launch_bounds__(128) k_jkr_mlp(StepParams P) {
 // a deferred list (contact_eval returns true) and k_contact_deferred
 // evaluates the deferred pairs densely; each pair writes the same result slots
 // in either pass, so the outcome does not depend on the order.
+// One contact result (force and torque on the row's particle, times its
+// visit count) into its record: FP64 in the FP64 form; FP32 in the mixed form,
+// whose pair forces are FP32 values (24 bytes a record instead of 48; the
+// per-particle sums stay FP64). Pairs the mixed form evaluates in FP64 (the
+// JKR fold band, decisions within FP32 rounding) are rounded once here.
+__device__ __forceinline__ void put_result(const StepParams& P, uint32_t rec, V f, V t, int visits) {
+  if (visits != 1) {  // x * 1 = x: no FP64 multiply for the common single visit
+    const double s = (double)visits;
+    f = f * s;
+    t = t * s;
+  }
+  if (P.prec == 1) {
+    float2* o = reinterpret_cast<float2*>(P.cresf + 6 * (size_t)rec);
+    o[0] = make_float2((float)f.x, (float)f.y);
+    o[1] = make_float2((float)f.z, (float)t.x);
+    o[2] = make_float2((float)t.y, (float)t.z);
+  } else {
+    double2* o = reinterpret_cast<double2*>(P.cres + 6 * (size_t)rec);
+    o[0] = make_double2(f.x, f.y);
+    o[1] = make_double2(f.z, t.x);
+    o[2] = make_double2(t.y, t.z);
+  }
+}
+
 template <bool PHYS, bool HIST, typename R>
 __device__ __forceinline__ bool contact_eval(const StepParams& P, const Bank& B, uint32_t t, bool first_pass,
                                              bool& excess, uint32_t* tally) {
@@ -1228,15 +1251,7 @@ __device__ __forceinline__ bool contact_eval(const StepParams& P, const Bank& B,
     hk[2 * plane] = 0.0;
   }
   if (P.debug) P.dbgMult[hik] = (uint8_t)(in ? vij : 0);
-  double* out = P.cres + 6 * (size_t)(P.coff[k] + c);
-  if (vij == 1) {  // x * 1 = x: no FP64 multiply for the common single visit
-    out[0] = fc.x; out[1] = fc.y; out[2] = fc.z;
-    out[3] = tc.x; out[4] = tc.y; out[5] = tc.z;
-  } else {
-    const double sv = (double)vij;
-    out[0] = fc.x * sv; out[1] = fc.y * sv; out[2] = fc.z * sv;
-    out[3] = tc.x * sv; out[4] = tc.y * sv; out[5] = tc.z * sv;
-  }
+  put_result(P, P.coff[k] + c, fc, tc, vij);
   if (vji > 0) {
     const uint32_t nj = P.ccnt[j];
     const CRec* rj = P.crec + (size_t)j * P.cap;
@@ -1250,15 +1265,7 @@ __device__ __forceinline__ bool contact_eval(const StepParams& P, const Bank& B,
       } else {
         t2 = cross(nrm * xj4.w, f2);
       }
-      double* o2 = P.cres + 6 * (size_t)(P.coff[j] + c2);
-      if (vji == 1) {
-        o2[0] = f2.x; o2[1] = f2.y; o2[2] = f2.z;
-        o2[3] = t2.x; o2[4] = t2.y; o2[5] = t2.z;
-      } else {
-        const double s2 = (double)vji;
-        o2[0] = f2.x * s2; o2[1] = f2.y * s2; o2[2] = f2.z * s2;
-        o2[3] = t2.x * s2; o2[4] = t2.y * s2; o2[5] = t2.z * s2;
-      }
+      put_result(P, P.coff[j] + c2, f2, t2, vji);
       const size_t h2 = (size_t)j * P.cap + (rj[c2].mv & 0xFFFFu);
       if (HIST) {
         B.hist[h2] = -hk[0];
@@ -1436,46 +1443,36 @@ __device__ __forceinline__ void finish_particle(const StepParams& P, const Bank&
   B.tq[k] = D4{plus_zero(T.x), plus_zero(T.y), plus_zero(T.z), 0.0};
 }
 
-// One block per tile of ACC_TILE slots (the tiles k_accum_order sorts
-// within): the tile's contact results are contiguous in cres (offsets are the
-// scan of the per-slot counts in slot order), so the block stages them in
-// shared memory with coalesced loads, ACC_WIN records per round, and each
-// thread sums its own slot's records from there in list order (the same sums
-// as reading them one by one). Threads take the tile's slots in the order
-// aorder gives (similar list lengths per warp).
-constexpr uint32_t ACC_WIN = 1024;  // 48 KB of FP64 results per round
-
-__global__ void __launch_bounds__(ACC_TILE) k_accumulate(StepParams P) {
+// Threads take the slots in the order aorder gives (tiles of 256 sorted by
+// list length, particles in triangle cells last). The contact results are
+// FP64 records (the FP64 form) or FP32 records (the mixed form, whose pair
+// forces are FP32 values); either way the sums are FP64, in list order.
+template <bool F32REC>
+__global__ void __launch_bounds__(256) k_accumulate(StepParams P) {
   Ctrl* C = P.ctrl;
   if (C->halt) return;
   const Bank B = P.bank[C->bank];
   const int lane = threadIdx.x & 31;
-  __shared__ double2 srec[3 * ACC_WIN];
-  for (int base = blockIdx.x * (int)ACC_TILE; base < P.n; base += gridDim.x * (int)ACC_TILE) {
-    const int i = base + (int)threadIdx.x;
-    const int last = min(base + (int)ACC_TILE, P.n) - 1;
-    const uint32_t R0 = P.coff[base], R1 = P.coff[last] + P.ccnt[last];
-    const int k = i < P.n ? (int)P.aorder[i] : -1;
-    uint32_t r0 = 0, r1 = 0;
-    if (k >= 0) {
-      r0 = P.coff[k];
-      r1 = r0 + P.ccnt[k];
-    }
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n; i += gridDim.x * blockDim.x) {
+    const int k = (int)P.aorder[i];
+    if (B.flags[k] & PF_DEAD) continue;
     V F = vmk(0.0, 0.0, 0.0), T = vmk(0.0, 0.0, 0.0);
-    const double2* src = reinterpret_cast<const double2*>(P.cres);
-    for (uint32_t w0 = R0; w0 < R1; w0 += ACC_WIN) {
-      const uint32_t w1 = min(w0 + ACC_WIN, R1);
-      __syncthreads();  // the previous round is consumed
-      for (uint32_t q = threadIdx.x; q < 3 * (w1 - w0); q += ACC_TILE) srec[q] = src[3 * (size_t)w0 + q];
-      __syncthreads();
-      const uint32_t a = max(r0, w0), b = min(r1, w1);
-      for (uint32_t c = a; c < b; ++c) {
-        const double2 x0 = srec[3 * (c - w0)], x1 = srec[3 * (c - w0) + 1], x2 = srec[3 * (c - w0) + 2];
-        F = F + vmk(x0.x, x0.y, x1.x);
-        T = T + vmk(x1.y, x2.x, x2.y);
+    const uint32_t n = P.ccnt[k];
+    if (F32REC) {
+      const float2* res = reinterpret_cast<const float2*>(P.cresf + 6 * (size_t)P.coff[k]);
+      for (uint32_t c = 0; c < n; ++c) {
+        const float2 r0 = res[3 * c], r1 = res[3 * c + 1], r2 = res[3 * c + 2];
+        F = F + vmk((double)r0.x, (double)r0.y, (double)r1.x);
+        T = T + vmk((double)r1.y, (double)r2.x, (double)r2.y);
+      }
+    } else {
+      const double2* res = reinterpret_cast<const double2*>(P.cres + 6 * (size_t)P.coff[k]);
+      for (uint32_t c = 0; c < n; ++c) {
+        const double2 r0 = res[3 * c], r1 = res[3 * c + 1], r2 = res[3 * c + 2];
+        F = F + vmk(r0.x, r0.y, r1.x);
+        T = T + vmk(r1.y, r2.x, r2.y);
       }
     }
-    if (k < 0 || (B.flags[k] & PF_DEAD)) continue;
     // wall pretests: the first WALL_CAND_CAP triangles that pass are kept
     // for k_accumulate_walls (a count above the cap says there are more)
     uint32_t nc = 0;
@@ -1759,8 +1756,8 @@ static int launch_contact_path(const StepParams& P, cudaStream_t s) {
     else k_contact_deferred<true, false, double><<<P.nsm * 8, 128, 0, s>>>(P);
     ++launched;
   }
-  (void)ba;  // one block per tile of ACC_TILE slots
-  k_accumulate<<<shaped_grid((uint64_t)P.n, ACC_TILE, cap), ACC_TILE, 0, s>>>(P);
+  if (P.prec == 1) k_accumulate<true><<<shaped_grid((uint64_t)P.n, ba, cap), ba, 0, s>>>(P);
+  else k_accumulate<false><<<shaped_grid((uint64_t)P.n, ba, cap), ba, 0, s>>>(P);
   if (P.ntri > 0) {  // over the queue k_accumulate filled; its length is only known on the device
     k_accumulate_walls<<<shaped_grid((uint64_t)P.n, 128, P.nsm * 16), 128, 0, s>>>(P);
     ++launched;

@@ -139,6 +139,7 @@ struct StepParams {
   uint32_t* ctot;   // [0] records, [1] evaluating records, [2] network queue, [3] deferred pairs, [4] wall queue
   uint32_t* jfb;    // evaluating indices deferred to the reference-Newton pass (null: no deferral)
   double* cres;     // per record: force (3) and torque (3) on the row's particle
+  float* cresf;     // the same buffer as FP32 records (the mixed form: its pair forces are FP32 values)
   uint32_t* cpart;  // scan partials
   int nmodel, tmodel, mode, prec;
   int periodic[3];
