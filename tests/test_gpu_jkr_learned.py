@@ -257,5 +257,10 @@ def test_network_gain_over_method_without_it(rp, trained):
     print("force pass ms: " + ", ".join(f"{k} {v[0]:.4f}" for k, v in res.items()))
     assert abs(steps_with - 2.0) < 0.01
     assert steps_without >= 1.5 * steps_with, (steps_without, steps_with)
-    # certificates and the FP32 solve remove the reference's FP64 iterations
+    # certificates and the FP32 solve remove the reference's FP64 iterations;
+    # the network itself costs more than the FP32 Newton steps it saves on this
+    # GPU (its pass is tens of microseconds, the saved steps about one), so
+    # learned is not asserted to beat certified: the finding is reported
     assert res["learned"][0] < res["newton"][0], res
+    assert res["certified"][0] < res["newton"][0], res
+    print(f"learned / certified force pass: {res['learned'][0] / res['certified'][0]:.3f}")
