@@ -325,7 +325,7 @@ int Engine::alloc_slots(size_t n) {
   TRY(dalloc(&aorder_, na)); TRY(dalloc(&wq_, na)); TRY(dalloc(&wcand_, na * WALL_CAND_CAP));
   TRY(dalloc(&ccnt_, na)); TRY(dalloc(&ncomp_, na)); TRY(dalloc(&coff_, na)); TRY(dalloc(&poff_, na));
   TRY(dalloc(&nnet_, na)); TRY(dalloc(&noff_, na));
-  TRY(dalloc(&ctot_, 8)); TRY(dalloc(&cpart_, scan_parts_needed((uint32_t)na) + 16));
+  TRY(dalloc(&ctot_, 8)); TRY(dalloc(&cpart_, 3 * (size_t)scan_parts_needed((uint32_t)na) + 16));
   CK(cudaMemset(ctot_, 0, 8 * sizeof(uint32_t)));
   n_alloc_ = na;
   // lists must be re-allocated for the new slot count

@@ -1754,14 +1754,11 @@ static int launch_contact_path(const StepParams& P, cudaStream_t s) {
   if (P.mode == 0) k_contact_filter<false, false><<<g, bf, 0, s>>>(P);
   else if (hist) k_contact_filter<true, true><<<g, bf, 0, s>>>(P);
   else k_contact_filter<true, false><<<g, bf, 0, s>>>(P);
-  launch_exclusive_scan(nullptr, P.ccnt, P.coff, (uint32_t)P.n, P.cpart, P.ctot, s);
-  launch_exclusive_scan(nullptr, P.ncomp, P.poff, (uint32_t)P.n, P.cpart, P.ctot + 1, s);
+  // record offsets, evaluating-record offsets (and the network queue's) in one set of scans
   const bool learn = P.jkr_solver == 1 && P.nmodel == 3 && P.mlp != nullptr;
-  int launched = 10;
-  if (learn) {
-    launch_exclusive_scan(nullptr, P.nnet, P.noff, (uint32_t)P.n, P.cpart, P.ctot + 2, s);
-    launched += 3;
-  }
+  const ScanSet S{{P.ccnt, P.ncomp, P.nnet}, {P.coff, P.poff, P.noff}, {P.ctot, P.ctot + 1, P.ctot + 2}};
+  launch_exclusive_scan_set(S, learn ? 3 : 2, (uint32_t)P.n, P.cpart, s);
+  int launched = 7;
   k_contact_index<<<grid_for(P.n, 256), 256, 0, s>>>(P);
   if (learn) {
     k_jkr_mlp<<<P.nsm * 4, 128, 0, s>>>(P);
