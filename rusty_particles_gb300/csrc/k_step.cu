@@ -1016,13 +1016,6 @@ __device__ __forceinline__ bool sjkr_far_zero(const StepParams& P, const Law& L,
 // candidates and the ones that evaluate their pair (the lower slot of a pair
 // seen from both ends, or the only end that sees it). The pretest is
 // symmetric, so a pair seen from both ends is a candidate at both.
-//
-// FILTER_LANES lanes share a particle: they read its row in coalesced chunks,
-// test one entry each and place the chunk's candidates by ballot and
-// popcount, so the records keep row order (the results do not depend on the
-// mapping) while the lanes stay busy on the pretest.
-constexpr int FILTER_LANES = 8;
-
 template <bool PHYS, bool HIST>
 __global__ void __launch_bounds__(256) k_contact_filter(StepParams P) {
   Ctrl* C = P.ctrl;
@@ -1039,14 +1032,9 @@ __global__ void __launch_bounds__(256) k_contact_filter(StepParams P) {
   // the same for sJKR, whose zero region is explicit (no iteration to certify)
   const bool sdrop = P.nmodel == 4 && P.pretest && !P.debug && (P.tmodel == 0 || PHYS);
   const size_t plane = (size_t)P.n * P.cap;
-  constexpr int G = FILTER_LANES;
-  const int lane = threadIdx.x & 31, sub = lane & (G - 1), shift = lane & ~(G - 1);
-  const unsigned gmask = ((1u << G) - 1u) << shift;
-  const unsigned below = (1u << sub) - 1u;
-  const int ngroups = (int)((gridDim.x * blockDim.x) / G);
   // slots in the rebuild-time order (tiles of 256 sorted by list length), so
-  // the groups of a warp walk lists of similar length
-  for (int i = (int)((blockIdx.x * blockDim.x + threadIdx.x) / G); i < P.n; i += ngroups) {
+  // a warp's lanes walk lists of similar length
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n; i += gridDim.x * blockDim.x) {
     const int k = (int)P.aorder[i];
     uint32_t nrec = 0, ncmp = 0, nnet = 0;
     if (!(B.flags[k] & PF_DEAD)) {
@@ -1062,39 +1050,33 @@ __global__ void __launch_bounds__(256) k_contact_filter(StepParams P) {
       const uint32_t cnt = B.ncnt[k];
       const uint32_t* row = B.nbr + (size_t)k * P.cap;
       CRec* out = P.crec + (size_t)k * P.cap;
-      for (uint32_t m0 = 0; m0 < cnt; m0 += G) {
-        const uint32_t m = m0 + (uint32_t)sub;
+      for (uint32_t m = 0; m < cnt; ++m) {
+        const uint32_t j = row[m];
+        const size_t hi = (size_t)k * P.cap + m;
         int vij = 0, vji = 0;
-        uint32_t j = 0;
-        if (m < cnt) {
-          j = row[m];
-          const float4 xjf = B.xf[j];
-          if (!(P.pretest && pretest_far(P, xif, Xi, xjf, adh)) &&
-              !(zdrop && jkr_far_zero(P, lw.jkr_Cf, xif, Xi, xjf)) && !(sdrop && sjkr_far_zero(P, lw, xif, Xi, xjf))) {
-            if (PHYS) {
-              vij = vji = 1;
+        const float4 xjf = B.xf[j];
+        if (!(P.pretest && pretest_far(P, xif, Xi, xjf, adh)) && !(zdrop && jkr_far_zero(P, lw.jkr_Cf, xif, Xi, xjf)) &&
+            !(sdrop && sjkr_far_zero(P, lw, xif, Xi, xjf))) {
+          if (PHYS) {
+            vij = vji = 1;
+          } else {
+            const unsigned long long cj = (unsigned long long)__double_as_longlong(B.wc[j].w);
+            if (cj == ci) {
+              vij = vji = same;
             } else {
-              const unsigned long long cj = (unsigned long long)__double_as_longlong(B.wc[j].w);
-              if (cj == ci) {
-                vij = vji = same;
-              } else {
-                vij = ref_visits(P, ci, cj);
-                vji = ref_visits(P, cj, ci);
-              }
+              vij = ref_visits(P, ci, cj);
+              vji = ref_visits(P, cj, ci);
             }
           }
         }
-        const bool rec = vij > 0;
-        const bool evaluates = rec && !(vji > 0 && (uint32_t)k > j);
-        const bool net = learn && evaluates && jkr_net_hint(P, lw.jkr_Cf, xif, B.xf[j]);
-        const unsigned brec = (__ballot_sync(gmask, rec) & gmask) >> shift;
-        const unsigned bcmp = (__ballot_sync(gmask, evaluates) & gmask) >> shift;
-        const unsigned bnet = (__ballot_sync(gmask, net) & gmask) >> shift;
-        if (rec) {
-          out[nrec + __popc(brec & below)] =
-              CRec{j, m | ((uint32_t)vij << 16) | ((uint32_t)vji << 24) | (net ? CREC_NET : 0u)};
-        } else if (m < cnt) {
-          const size_t hi = (size_t)k * P.cap + m;
+        if (vij > 0) {
+          const bool evaluates = !(vji > 0 && (uint32_t)k > j);
+          const uint32_t net = (learn && evaluates && jkr_net_hint(P, lw.jkr_Cf, xif, xjf)) ? CREC_NET : 0u;
+          out[nrec] = CRec{j, m | ((uint32_t)vij << 16) | ((uint32_t)vji << 24) | net};
+          ++nrec;
+          if (evaluates) ++ncmp;
+          if (net) ++nnet;
+        } else {
           if (HIST) {
             B.hist[hi] = 0.0;
             B.hist[plane + hi] = 0.0;
@@ -1102,16 +1084,11 @@ __global__ void __launch_bounds__(256) k_contact_filter(StepParams P) {
           }
           if (P.debug) P.dbgMult[hi] = 0;
         }
-        nrec += __popc(brec);
-        ncmp += __popc(bcmp);
-        nnet += __popc(bnet);
       }
     }
-    if (sub == 0) {
-      P.ccnt[k] = nrec;
-      P.ncomp[k] = ncmp;
-      if (learn_any) P.nnet[k] = nnet;
-    }
+    P.ccnt[k] = nrec;
+    P.ncomp[k] = ncmp;
+    if (learn_any) P.nnet[k] = nnet;
   }
 }
 
@@ -1749,7 +1726,7 @@ template <typename R>
 static int launch_contact_path(const StepParams& P, cudaStream_t s) {
   const int bf = P.bs_filter > 0 ? P.bs_filter : 128, bc = P.bs_force > 0 ? P.bs_force : 128,
             ba = P.bs_accum > 0 ? P.bs_accum : 128, cap = P.grid_cap > 0 ? P.grid_cap : P.nsm * 64;
-  const int g = shaped_grid((uint64_t)P.n * FILTER_LANES, bf, cap);  // FILTER_LANES lanes per particle
+  const int g = shaped_grid((uint64_t)P.n, bf, cap);
   const bool hist = P.mode == 1 && P.tmodel != 0;
   if (P.mode == 0) k_contact_filter<false, false><<<g, bf, 0, s>>>(P);
   else if (hist) k_contact_filter<true, true><<<g, bf, 0, s>>>(P);
