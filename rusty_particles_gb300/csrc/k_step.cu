@@ -320,7 +320,8 @@ __device__ __forceinline__ T3<R> spring_coulomb(R fn, T3<R> rv, T3<R> n, T3<R>& 
 template <typename R, bool PHYS, bool HIST>
 __device__ __forceinline__ bool pair_contact(const StepParams& P, const Law& L, V d, double d2, double rsum, double ri,
                                              double rj, double mi, double mj, V vi, V vj, V wi, V wj, double* hist,
-                                             size_t plane, V& fc_out, V& tc_out, V& n_out, bool& excess,
+                                             size_t plane, T3<R>& fc_out, T3<R>& tc_out, T3<R>& n_out,
+                                             bool& excess,
                                              float guess = -1.0f, uint32_t* tally = nullptr,
                                              bool* deferred = nullptr, bool newton = false) {
   constexpr bool F32 = sizeof(R) == sizeof(float);
@@ -478,9 +479,9 @@ __device__ __forceinline__ bool pair_contact(const StepParams& P, const Law& L, 
   }
   const T3<R> fc = ft_zero ? t3(plus_zero(fnv.x), plus_zero(fnv.y), plus_zero(fnv.z)) : fnv + ft;
   const T3<R> tc = cross(ra, fc);
-  fc_out = cvt<double>(fc);
-  tc_out = cvt<double>(tc);
-  n_out = cvt<double>(n);
+  fc_out = fc;
+  tc_out = tc;
+  n_out = n;
   return true;
 }
 
@@ -573,7 +574,7 @@ __global__ void __launch_bounds__(256) k_first_half(StepParams P) {
       // first half kick into one kick of a dt
       const double kdt = (!KAHAN && FUSE) ? dt : hdt;
       dv = a * kdt;
-      dw = (tau * inv_inertia) * kdt;
+      dw = KAHAN ? (tau * inv_inertia) * kdt : tau * (inv_inertia * kdt);
       if (KAHAN && FUSE) {
         kahan_add(v, vres, dv);
         kahan_add(w, wres, dw);
@@ -863,10 +864,15 @@ __global__ void __launch_bounds__(128) k_force(StepParams P) {
         if (visits > 0) {
           const D4 vj4 = B.vm[j];
           V fc, tc, nrm;
-          if (!pair_contact<R, PHYS, HIST>(P, lw, d, d2, rsum, ri, rj, mi, vj4.w, vi, xyz(vj4), wi, xyz(wj4),
-                                           HIST ? B.hist + hi : nullptr, plane, fc, tc, nrm, excess))
+          T3<R> fr, tr, nr;
+          if (pair_contact<R, PHYS, HIST>(P, lw, d, d2, rsum, ri, rj, mi, vj4.w, vi, xyz(vj4), wi, xyz(wj4),
+                                          HIST ? B.hist + hi : nullptr, plane, fr, tr, nr, excess)) {
+            fc = cvt<double>(fr);
+            tc = cvt<double>(tr);
+          } else {
             pair_contact<double, PHYS, HIST>(P, lw, d, d2, rsum, ri, rj, mi, vj4.w, vi, xyz(vj4), wi, xyz(wj4),
                                              HIST ? B.hist + hi : nullptr, plane, fc, tc, nrm, excess);
+          }
           for (int t = 0; t < visits; ++t) {
             F = F + fc;
             T = T + tc;
@@ -1017,7 +1023,7 @@ __device__ __forceinline__ bool sjkr_far_zero(const StepParams& P, const Law& L,
 // seen from both ends, or the only end that sees it). The pretest is
 // symmetric, so a pair seen from both ends is a candidate at both.
 template <bool PHYS, bool HIST>
-__global__ void __launch_bounds__(256) k_contact_filter(StepParams P) {
+__global__ void __launch_bounds__(256, 4) k_contact_filter(StepParams P) {
   Ctrl* C = P.ctrl;
   if (C->halt) return;
   const Bank B = P.bank[C->bank];
@@ -1193,9 +1199,12 @@ __global__ void __launch_bounds__(128) k_jkr_mlp(StepParams P) {
 // whose pair forces are FP32 values (24 bytes a record instead of 48; the
 // per-particle sums stay FP64). Pairs the mixed form evaluates in FP64 (the
 // JKR fold band, decisions within FP32 rounding) are rounded once here.
-__device__ __forceinline__ void put_result(const StepParams& P, uint32_t rec, V f, V t, int visits) {
-  if (visits != 1) {  // x * 1 = x: no FP64 multiply for the common single visit
-    const double s = (double)visits;
+// The FP32 form's results stay FP32 from the law to the record (a visit
+// count times an FP32 value rounds the same in FP32 as in FP64).
+template <typename R>
+__device__ __forceinline__ void put_result(const StepParams& P, uint32_t rec, T3<R> f, T3<R> t, int visits) {
+  if (visits != 1) {  // x * 1 = x: no multiply for the common single visit
+    const R s = (R)visits;
     f = f * s;
     t = t * s;
   }
@@ -1232,7 +1241,7 @@ __device__ __forceinline__ bool contact_eval(const StepParams& P, const Bank& B,
   const bool in = d2 < cut * cut;
   const size_t hik = (size_t)k * P.cap + m;
   double* hk = HIST ? B.hist + hik : nullptr;
-  V fc = vmk(0.0, 0.0, 0.0), tc = fc, nrm = fc;
+  T3<R> fc = t3(R(0), R(0), R(0)), tc = fc, nrm = fc;
   if (in) {
     const D4 vi4 = B.vm[k], wi4 = B.wc[k], vj4 = B.vm[j], wj4 = B.wc[j];
     const Law lw = law_of(P, B, (int)k);
@@ -1240,10 +1249,15 @@ __device__ __forceinline__ bool contact_eval(const StepParams& P, const Bank& B,
     const bool can_defer = first_pass && P.jfb != nullptr;
     if (!pair_contact<R, PHYS, HIST>(P, lw, d, d2, rsum, xi4.w, xj4.w, vi4.w, vj4.w, xyz(vi4), xyz(vj4), xyz(wi4),
                                      xyz(wj4), hk, plane, fc, tc, nrm, excess, guess, tally,
-                                     can_defer ? &deferred : nullptr, !first_pass))
+                                     can_defer ? &deferred : nullptr, !first_pass)) {
+      V fd, td, nd;
       pair_contact<double, PHYS, HIST>(P, lw, d, d2, rsum, xi4.w, xj4.w, vi4.w, vj4.w, xyz(vi4), xyz(vj4),
-                                       xyz(wi4), xyz(wj4), hk, plane, fc, tc, nrm, excess, guess, nullptr, nullptr,
+                                       xyz(wi4), xyz(wj4), hk, plane, fd, td, nd, excess, guess, nullptr, nullptr,
                                        !first_pass);
+      fc = cvt<R>(fd);
+      tc = cvt<R>(td);
+      nrm = cvt<R>(nd);
+    }
     if (deferred) return true;
   } else if (HIST) {
     hk[0] = 0.0;
@@ -1257,14 +1271,8 @@ __device__ __forceinline__ bool contact_eval(const StepParams& P, const Bank& B,
     const CRec* rj = P.crec + (size_t)j * P.cap;
     for (uint32_t c2 = 0; c2 < nj; ++c2) {
       if (rj[c2].j != k) continue;
-      const V f2 = -fc;
-      V t2;
-      if (sizeof(R) == sizeof(float)) {
-        const Vf raj = cvt<float>(nrm) * (float)xj4.w;
-        t2 = cvt<double>(cross(raj, cvt<float>(f2)));
-      } else {
-        t2 = cross(nrm * xj4.w, f2);
-      }
+      const T3<R> f2 = -fc;
+      const T3<R> t2 = cross(nrm * (R)xj4.w, f2);
       put_result(P, P.coff[j] + c2, f2, t2, vji);
       const size_t h2 = (size_t)j * P.cap + (rj[c2].mv & 0xFFFFu);
       if (HIST) {
