@@ -183,6 +183,52 @@ def test_one_step_fine_floor_many_wall_contacts(rp, oracle_mod):
     assert np.count_nonzero(Fo[:, 1] > 0) == k // 2
 
 
+def test_walls_across_list_rebuilds(rp, oracle_mod):
+    # spheres sliding at 0.5 m/s over a floor of 4 mm triangles with a small
+    # Verlet skin: the lists, and each sphere's list of nearby triangles, are
+    # rebuilt every few steps while the wall contacts move from triangle to
+    # triangle; every step matches the oracle (src/simulation.rs:464-523)
+    lo, hi = (-0.1, -0.05, -0.1), (0.1, 0.1, 0.1)
+    m = 25
+    xs = np.linspace(-0.05, 0.05, m + 1)
+    v = []
+    for i in range(m):
+        for j in range(m):
+            a, b, c, d = (xs[i], 0, xs[j]), (xs[i + 1], 0, xs[j]), (xs[i], 0, xs[j + 1]), (xs[i + 1], 0, xs[j + 1])
+            v += [a + c + b, b + c + d]
+    v = np.array(v, np.float32).astype(np.float64)
+    n = np.tile([0.0, 1.0, 0.0], (len(v), 1))
+    rng = np.random.default_rng(43)
+    g = np.stack(np.meshgrid(np.arange(6), np.arange(6), indexing="ij"), -1).reshape(-1, 2)
+    k = len(g)
+    r = rng.uniform(0.004, 0.006, k)
+    x = np.stack([-0.035 + g[:, 0] * 0.013, r - rng.uniform(0.0001, 0.0003, k), -0.035 + g[:, 1] * 0.013], 1)
+    vel = np.zeros((k, 3))
+    vel[:, 0] = 0.5
+    vel[:, 2] = rng.normal(0, 0.1, k)
+    st = {"position": x, "radius": r, "mass": 2500.0 * 4.0 / 3.0 * np.pi * r ** 3, "velocity": vel,
+          "angular_velocity": rng.normal(0, 1.0, (k, 3)), "acceleration": np.zeros((k, 3)),
+          "torque": np.zeros((k, 3)), "fixed": np.zeros(k, np.uint8)}
+    wall = (1e8, 0.25, 7800.0, 0.3, 0.6, 0.0)
+    dt = 1e-5
+    o = pu.oracle_sim(oracle_mod, st, dt, lo, hi, 1, 0, tris=(v, n), cell=0.02, wall=wall)
+    g = pu.gpu_sim(rp, st, dt, lo, hi, 1, 0, tris=(v, n), cell=0.02, wall=wall)
+    g.set_skin(5e-5)  # half of it in five steps at 0.5 m/s
+    for step in range(40):
+        o.step()
+        g.step()
+        so, sg = o.state(), g.get_state()
+        assert float(np.max(np.abs(sg["position"] - so["x"]))) < 1e-12, step
+        Fo, To = o.last_forces()
+        Fg, Tg = g.debug_forces()
+        FS, TS = o.last_force_scale()
+        m_ = FS > 0
+        assert np.count_nonzero(m_) == k  # every sphere touches the floor
+        assert float((np.linalg.norm(Fg - Fo, axis=1)[m_] / FS[m_]).max()) <= 1e-9, step
+        assert float((np.linalg.norm(Tg - To, axis=1)[m_] / TS[m_]).max()) <= 1e-9, step
+    assert g.stats()["neighbor_rebuilds"] >= 6
+
+
 def test_one_step_physical_mindlin(rp, oracle_mod):
     lo, hi = (-0.25, -0.25, -0.25), (0.25, 0.25, 0.25)
     st = pu.random_bed(31, 2000, lo, hi, 0.008, 0.012)
