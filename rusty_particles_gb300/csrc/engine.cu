@@ -122,7 +122,7 @@ void Engine::free_device() {
   dfree(rb_.ka); dfree(rb_.va); dfree(rb_.kb); dfree(rb_.vb); dfree(rb_.hist); dfree(rb_.part);
   dfree(rb_.cstart); dfree(rb_.cend); dfree(kraw_);
   dfree(dbgF_); dfree(dbgT_); dfree(dbgMult_); dfree(ke_);
-  dfree(crec_); dfree(clist_); dfree(cres_); dfree(ccnt_); dfree(aorder_); dfree(wq_); dfree(wcand_); dfree(wlist_); dfree(wlcnt_); dfree(ncomp_); dfree(coff_); dfree(poff_);
+  dfree(crec_); dfree(clist_); dfree(cres_); dfree(ccnt_); dfree(aorder_); dfree(wq_); dfree(wcand_); dfree(ncomp_); dfree(coff_); dfree(poff_);
   dfree(ctot_); dfree(cpart_);
   dfree(tri_d_); dfree(tstart_d_); dfree(titems_d_); dfree(glaw_d_); dfree(motions_d_);
   dfree(mlp_d_); dfree(jq_); dfree(jguess_); dfree(nnet_); dfree(noff_); dfree(jfb_);
@@ -323,7 +323,6 @@ int Engine::alloc_slots(size_t n) {
   TRY(dalloc(&rb_.part, scan_parts_needed(std::max<uint32_t>(hn, (uint32_t)na)) + 16));
   TRY(dalloc(&dbgF_, 3 * na)); TRY(dalloc(&dbgT_, 3 * na));
   TRY(dalloc(&aorder_, na)); TRY(dalloc(&wq_, na)); TRY(dalloc(&wcand_, na * WALL_CAND_CAP));
-  TRY(dalloc(&wlist_, na * WALL_LIST_CAP)); TRY(dalloc(&wlcnt_, na));
   TRY(dalloc(&ccnt_, na)); TRY(dalloc(&ncomp_, na)); TRY(dalloc(&coff_, na)); TRY(dalloc(&poff_, na));
   TRY(dalloc(&nnet_, na)); TRY(dalloc(&noff_, na));
   TRY(dalloc(&ctot_, 8)); TRY(dalloc(&cpart_, 3 * (size_t)scan_parts_needed((uint32_t)na) + 16));
@@ -438,8 +437,6 @@ void Engine::refresh_list_ptrs() {
   P_.aorder = aorder_;
   P_.wq = wq_;
   P_.wcand = wcand_;
-  P_.wlist = wlist_;
-  P_.wlcnt = wlcnt_;
   P_.ncomp = ncomp_;
   P_.coff = coff_;
   P_.poff = poff_;
@@ -559,13 +556,7 @@ int Engine::build_params() {
     TRY(dalloc(&rb_.cend, P.fncells));
     fcells_alloc_ = P.fncells;
   }
-  // A particle's wall list holds the triangles within its radius plus half
-  // the skin (with a margin) at the list rebuild: until the next rebuild it
-  // moves less than half the skin, so every triangle it can touch is listed.
-  // The triangle grid covers that reach.
-  const double wl_reach = 0.5 * skin * 1.001;
-  P.wl_reachf = (float)wl_reach;
-  TRY(build_triangle_grid(rmax + wl_reach));
+  TRY(build_triangle_grid(rmax));
   P.dbgF = dbgF_;
   P.dbgT = dbgT_;
   P.ctrl = ctrl_;

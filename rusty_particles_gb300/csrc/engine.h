@@ -147,7 +147,6 @@ class Engine {
   uint32_t* aorder_ = nullptr;  // k_accumulate visiting order (set at every list rebuild)
   uint2* wq_ = nullptr;         // wall queue of the accumulate pass
   uint32_t* wcand_ = nullptr;   // wall candidates per slot
-  uint32_t *wlist_ = nullptr, *wlcnt_ = nullptr;  // wall lists per slot (rebuilt with the neighbour lists)
   uint32_t *ctot_ = nullptr, *cpart_ = nullptr;
   double* cres_ = nullptr;
   void refresh_list_ptrs();

@@ -700,8 +700,9 @@ __device__ __forceinline__ bool tri_cell_range(const StepParams& P, float4 xf, u
 
 // FP32 pretest of a sphere (centre xf, radius rf = xf.w, largest |coordinate|
 // xmag, group gi) against a triangle: false when it cannot touch it.
-__device__ __forceinline__ bool wall_pretest_r(const TriRec& tr, uint32_t gi, float4 xf, float xmag, float rf) {
+__device__ __forceinline__ bool wall_pretest(const TriRec& tr, uint32_t gi, float4 xf, float xmag) {
   if (tr.group != GROUP_ALL && tr.group != gi) return false;
+  const float rf = xf.w;
   // FP32 rounding of n, n.v0 and x moves n.x - n.v0 by at most
   // ~3e-7 (|x| + |n.v0|) + 1.1e-7 |x - v0|; the margin is larger
   const float4 pl = tr.plane;
@@ -718,9 +719,6 @@ __device__ __forceinline__ bool wall_pretest_r(const TriRec& tr, uint32_t gi, fl
   const float me = mrg + 4e-7f * tr.bound.x;
   const float hl = fmaxf(hd - mrg, 0.0f), sl = fmaxf(s - me, 0.0f);
   return !(hl * hl + sl * sl > rf * rf * (1.0f + 1e-6f));
-}
-__device__ __forceinline__ bool wall_pretest(const TriRec& tr, uint32_t gi, float4 xf, float xmag) {
-  return wall_pretest_r(tr, gi, xf, xmag, xf.w);
 }
 
 // The FP64 contact of a sphere with a triangle that passed the pretest:
@@ -1364,58 +1362,15 @@ __global__ void __launch_bounds__(128) k_contact_deferred(StepParams P) {
 constexpr uint32_t ACC_BINS = 128;
 constexpr uint32_t ACC_TILE = 256;
 
-// The wall list of each slot, at a list rebuild (the bank the rebuild fills):
-// the triangles of its triangle-grid cell, in mesh order, that the FP32
-// pretest cannot rule out for the radius grown by the reach P.wl_reachf
-// (half the skin) and the mirror's rounding; up to WALL_LIST_CAP of them, or
-// WALL_LIST_CELL when there are more (the step then walks the cell).
-__global__ void k_build_wlist(StepParams P) {
-  {
-    volatile const Ctrl* c = P.ctrl;
-    if (c->rebuild == 0 || c->halt != 0) return;
-  }
-  const Bank B = P.bank[P.ctrl->bank ^ 1];
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < P.n; k += gridDim.x * blockDim.x) {
-    uint32_t cnt = 0;
-    uint32_t s, e;
-    const float4 xf = B.xf[k];
-    if (!(B.flags[k] & PF_DEAD) && tri_cell_range(P, xf, s, e)) {
-      const float xmag = fmaxf(fmaxf(fabsf(xf.x), fabsf(xf.y)), fabsf(xf.z));
-      const float rl = xf.w + P.wl_reachf + 1e-6f * (1.0f + xmag);
-      const uint32_t gi = P.ngroups > 1 ? B.grp[k] : 0u;
-      uint32_t* out = P.wlist + (size_t)k * WALL_LIST_CAP;
-      for (uint32_t t = s; t < e; ++t) {
-        const uint32_t id = P.titems[t];
-        if (!wall_pretest_r(P.tri[id], gi, xf, xmag, rl)) continue;
-        if (cnt == WALL_LIST_CAP) {
-          cnt = WALL_LIST_CELL;
-          break;
-        }
-        out[cnt++] = id;
-      }
-    }
-    P.wlcnt[k] = cnt;
-  }
-}
-
-// The triangles a slot tests this step: its wall list, or (a list past the
-// cap) the triangles of its current grid cell; [s, e) into `ids`.
-__device__ __forceinline__ void wall_source(const StepParams& P, int k, float4 xf, const uint32_t*& ids, uint32_t& s,
-                                            uint32_t& e) {
-  const uint32_t wc = P.wlcnt[k];
-  if (wc != WALL_LIST_CELL) {
-    ids = P.wlist + (size_t)k * WALL_LIST_CAP;
-    s = 0;
-    e = wc;
-  } else {
-    ids = P.titems;
-    if (!tri_cell_range(P, xf, s, e)) s = e = 0;
-  }
+__device__ __forceinline__ bool tri_cell_nonempty(const StepParams& P, float4 xf) {
+  uint32_t s, e;
+  return tri_cell_range(P, xf, s, e) && e > s;
 }
 
 // The visiting order of k_accumulate, at a list rebuild: within each tile of
-// 256 slots a counting sort by (a wall list is not empty, Verlet-list
-// length), dead slots after the live ones. Reads the bank the rebuild fills.
+// 256 slots a counting sort by (triangles listed in the triangle-grid cell,
+// Verlet-list length), dead slots after the live ones. Reads the bank the
+// rebuild fills.
 __global__ void __launch_bounds__(ACC_TILE) k_accum_order(StepParams P) {
   {
     volatile const Ctrl* c = P.ctrl;
@@ -1432,7 +1387,7 @@ __global__ void __launch_bounds__(ACC_TILE) k_accum_order(StepParams P) {
         key = 63;
       } else {
         key = min(B.ncnt[k0], 62u);
-        if (P.ntri > 0 && P.wlcnt[k0] != 0u) key += 64;
+        if (P.ntri > 0 && tri_cell_nonempty(P, B.xf[k0])) key += 64;
       }
     }
     for (uint32_t i = threadIdx.x; i < ACC_BINS; i += blockDim.x) bins[i] = 0;
@@ -1463,13 +1418,8 @@ __global__ void __launch_bounds__(ACC_TILE) k_accum_order(StepParams P) {
 
 int launch_accum_order(const StepParams& P, cudaStream_t s) {
   const uint64_t tiles = ((uint64_t)P.n + ACC_TILE - 1) / ACC_TILE;
-  int launched = 1;
-  if (P.ntri > 0) {
-    k_build_wlist<<<grid_for(P.n, 128), 128, 0, s>>>(P);
-    ++launched;
-  }
   k_accum_order<<<(int)std::min<uint64_t>(std::max<uint64_t>(tiles, 1), (uint64_t)P.nsm * 64ull), ACC_TILE, 0, s>>>(P);
-  return launched;
+  return 1;
 }
 
 // Exclusive scan of one value per thread (blockDim.x a multiple of 32, at
@@ -1547,17 +1497,15 @@ __global__ void __launch_bounds__(256) k_accumulate(StepParams P) {
     // wall pretests: the first WALL_CAND_CAP triangles that pass are kept
     // for k_accumulate_walls (a count above the cap says there are more)
     uint32_t nc = 0;
-    if (P.ntri > 0 && P.wlcnt[k] != 0u) {
+    if (P.ntri > 0) {
       const float4 xf = B.xf[k];
       uint32_t s, e;
-      const uint32_t* ids;
-      wall_source(P, k, xf, ids, s, e);
-      if (e > s) {
+      if (tri_cell_range(P, xf, s, e) && e > s) {
         const float xmag = fmaxf(fmaxf(fabsf(xf.x), fabsf(xf.y)), fabsf(xf.z));
         const uint32_t gi = P.ngroups > 1 ? B.grp[k] : 0u;
         uint32_t* out = P.wcand + (size_t)k * WALL_CAND_CAP;
         for (uint32_t t = s; t < e; ++t) {
-          const uint32_t id = ids[t];
+          const uint32_t id = P.titems[t];
           if (!wall_pretest(P.tri[id], gi, xf, xmag)) continue;
           if (nc == WALL_CAND_CAP) {
             ++nc;
@@ -1650,15 +1598,14 @@ __global__ void __launch_bounds__(256) k_accumulate_walls(StepParams P) {
     if (qe.y > WALL_CAND_CAP) {  // candidates past the cap, inline, still in mesh order
       const float4 xf = B.xf[k];
       uint32_t s = 0, e = 0;
-      const uint32_t* ids;
-      wall_source(P, k, xf, ids, s, e);  // the same source k_accumulate walked
+      tri_cell_range(P, xf, s, e);
       const float xmag = fmaxf(fmaxf(fabsf(xf.x), fabsf(xf.y)), fabsf(xf.z));
       const uint32_t gi = P.ngroups > 1 ? B.grp[k] : 0u;
       const D4 xi4 = B.xr[k], vi4 = B.vm[k], wi4 = B.wc[k];
       const Law L = law_of(P, B, k);
       uint32_t seen = 0;
       for (uint32_t t = s; t < e; ++t) {
-        const TriRec& tr = P.tri[ids[t]];
+        const TriRec& tr = P.tri[P.titems[t]];
         if (!wall_pretest(tr, gi, xf, xmag)) continue;
         if (seen++ < WALL_CAND_CAP) continue;  // evaluated in the dense rounds
         V fc, tc;

@@ -64,8 +64,6 @@ struct Law {
 };
 constexpr uint32_t GROUP_ALL = 0xFFFFFFFFu;
 constexpr uint32_t WALL_CAND_CAP = 8;  // wall candidates held per particle between the accumulate kernels
-constexpr uint32_t WALL_LIST_CAP = 8;  // triangles of a particle's wall list, set at each list rebuild
-constexpr uint32_t WALL_LIST_CELL = 0xFFFFFFFFu;  // wall-list count: more than the cap, use the grid cell
 
 // A rigid surface velocity V + W x (p - C) of a set of triangles whose geometry
 // stays put (a surface of revolution turning about its own axis, a belt). The
@@ -134,9 +132,6 @@ struct StepParams {
   uint32_t* aorder; // slots in the order k_accumulate visits them (a permutation within tiles of 256)
   uint2* wq;        // (slot, wall candidates) of the particles with a wall candidate; length ctot[4]
   uint32_t* wcand;  // per slot, the first WALL_CAND_CAP triangles that passed the wall pretest
-  uint32_t* wlist;  // per slot, WALL_LIST_CAP triangles within reach until the next list rebuild (mesh order)
-  uint32_t* wlcnt;  // per slot, their count, or WALL_LIST_CELL
-  float wl_reachf;  // how far beyond its radius a wall list reaches (half the skin, with a margin)
   uint32_t* ncomp;  // records that evaluate their pair (each pair once)
   uint32_t* coff;   // exclusive scan of ccnt: result offset of particle k
   uint32_t* poff;   // exclusive scan of ncomp

@@ -45,11 +45,7 @@ def test_device_grid_matches_restatement(rp, which):
     wl = bench.hopper_workload(n=5000) if which == "hopper" else bench.drum_workload(n=5000)
     sim = bench.make_sim(rp, wl)
     dims, lo, cell, start, items = device_grid(sim)
-    # the grid covers the largest radius plus the wall lists' reach, half the
-    # default Verlet skin (0.2 of the largest radius) with a 0.1 % margin
-    rmax = float(np.max(wl["radius"]))
-    skin = 0.1 * 2.0 * rmax
-    rdims, rlo, rcell, rstart, ritems = tg.triangle_grid(wl["tri_v"], rmax + 0.5 * skin * 1.001)
+    rdims, rlo, rcell, rstart, ritems = tg.triangle_grid(wl["tri_v"], float(np.max(wl["radius"])))
     assert dims == rdims
     np.testing.assert_array_equal(lo, rlo)
     assert cell == rcell
