@@ -122,10 +122,10 @@ void Engine::free_device() {
   dfree(rb_.ka); dfree(rb_.va); dfree(rb_.kb); dfree(rb_.vb); dfree(rb_.hist); dfree(rb_.part);
   dfree(rb_.cstart); dfree(rb_.cend); dfree(kraw_);
   dfree(dbgF_); dfree(dbgT_); dfree(dbgMult_); dfree(ke_);
-  dfree(crec_); dfree(clist_); dfree(cres_); dfree(ccnt_); dfree(aorder_); dfree(wq_); dfree(wcand_); dfree(ncomp_); dfree(coff_); dfree(poff_);
-  dfree(ctot_); dfree(cpart_);
+  dfree(crec_); dfree(clist_); dfree(cres_); dfree(ccnt_); dfree(aorder_); dfree(wq_); dfree(wcand_); dfree(coff_);
+  dfree(ctot_);
   dfree(tri_d_); dfree(tstart_d_); dfree(titems_d_); dfree(glaw_d_); dfree(motions_d_);
-  dfree(mlp_d_); dfree(jq_); dfree(jguess_); dfree(nnet_); dfree(noff_); dfree(jfb_);
+  dfree(mlp_d_); dfree(jq_); dfree(jguess_); dfree(jfb_);
   dfree(io_buf_); dfree(slot_of_); dfree(io_flag_); dfree(id_live_); dfree(id_pos_); dfree(slot_of_id_);
   dfree(id_part_);
   io_n_ = 0;
@@ -323,9 +323,8 @@ int Engine::alloc_slots(size_t n) {
   TRY(dalloc(&rb_.part, scan_parts_needed(std::max<uint32_t>(hn, (uint32_t)na)) + 16));
   TRY(dalloc(&dbgF_, 3 * na)); TRY(dalloc(&dbgT_, 3 * na));
   TRY(dalloc(&aorder_, na)); TRY(dalloc(&wq_, na)); TRY(dalloc(&wcand_, na * WALL_CAND_CAP));
-  TRY(dalloc(&ccnt_, na)); TRY(dalloc(&ncomp_, na)); TRY(dalloc(&coff_, na)); TRY(dalloc(&poff_, na));
-  TRY(dalloc(&nnet_, na)); TRY(dalloc(&noff_, na));
-  TRY(dalloc(&ctot_, 8)); TRY(dalloc(&cpart_, 3 * (size_t)scan_parts_needed((uint32_t)na) + 16));
+  TRY(dalloc(&ccnt_, na)); TRY(dalloc(&coff_, na));
+  TRY(dalloc(&ctot_, 8));
   CK(cudaMemset(ctot_, 0, 8 * sizeof(uint32_t)));
   n_alloc_ = na;
   // lists must be re-allocated for the new slot count
@@ -437,13 +436,8 @@ void Engine::refresh_list_ptrs() {
   P_.aorder = aorder_;
   P_.wq = wq_;
   P_.wcand = wcand_;
-  P_.ncomp = ncomp_;
   P_.coff = coff_;
-  P_.poff = poff_;
-  P_.nnet = nnet_;
-  P_.noff = noff_;
   P_.ctot = ctot_;
-  P_.cpart = cpart_;
 }
 
 // ------------------------------------------------------------ parameters

@@ -143,11 +143,11 @@ class Engine {
   uint8_t* dbgMult_ = nullptr;
   // contact-parallel force buffers
   CRec* crec_ = nullptr;
-  uint32_t *ccnt_ = nullptr, *ncomp_ = nullptr, *coff_ = nullptr, *poff_ = nullptr, *clist_ = nullptr;
+  uint32_t *ccnt_ = nullptr, *coff_ = nullptr, *clist_ = nullptr;
   uint32_t* aorder_ = nullptr;  // k_accumulate visiting order (set at every list rebuild)
   uint2* wq_ = nullptr;         // wall queue of the accumulate pass
   uint32_t* wcand_ = nullptr;   // wall candidates per slot
-  uint32_t *ctot_ = nullptr, *cpart_ = nullptr;
+  uint32_t *ctot_ = nullptr;
   double* cres_ = nullptr;
   void refresh_list_ptrs();
   double* ke_ = nullptr;
@@ -159,7 +159,6 @@ class Engine {
   MlpInfer* mlp_d_ = nullptr;
   uint2* jq_ = nullptr;
   float* jguess_ = nullptr;
-  uint32_t *nnet_ = nullptr, *noff_ = nullptr;
   size_t jq_alloc_ = 0;
   uint32_t* jfb_ = nullptr;  // pairs deferred to the reference-Newton pass
   size_t jfb_alloc_ = 0;

@@ -246,68 +246,6 @@ void launch_exclusive_scan(const Ctrl* gate, const uint32_t* in, uint32_t* out, 
   k_scan_down<<<nb, SC_BLOCK, 0, s>>>(gate, in, out, n, part);
 }
 
-// Up to three scans of the same length in one set of three launches
-// (blockIdx.y picks the array; the per-tile sums of array y live at
-// part + y * stride). Same results as launch_exclusive_scan on each.
-__global__ void __launch_bounds__(SC_BLOCK) k_scan_reduce_set(ScanSet S, uint32_t n, uint32_t* part,
-                                                               uint32_t stride) {
-  const uint32_t* in = S.in[blockIdx.y];
-  uint32_t base = blockIdx.x * SC_TILE + threadIdx.x * SC_ITEMS, s = 0;
-#pragma unroll
-  for (int i = 0; i < SC_ITEMS; ++i)
-    if (base + i < n) s += in[base + i];
-  __shared__ uint32_t tot;
-  block_exclusive_scan(s, &tot);
-  if (threadIdx.x == 0) part[(size_t)blockIdx.y * stride + blockIdx.x] = tot;
-}
-
-__global__ void __launch_bounds__(1024) k_scan_top_set(ScanSet S, uint32_t* part, uint32_t np, uint32_t stride) {
-  uint32_t* pp = part + (size_t)blockIdx.x * stride;
-  __shared__ uint32_t carry_s;
-  __shared__ uint32_t tot;
-  if (threadIdx.x == 0) carry_s = 0;
-  __syncthreads();
-  for (uint32_t base = 0; base < np; base += blockDim.x) {
-    uint32_t i = base + threadIdx.x;
-    uint32_t v = i < np ? pp[i] : 0u;
-    uint32_t ex = block_exclusive_scan(v, &tot);
-    uint32_t c = carry_s;
-    if (i < np) pp[i] = ex + c;
-    __syncthreads();
-    if (threadIdx.x == 0) carry_s = c + tot;
-    __syncthreads();
-  }
-  if (threadIdx.x == 0 && S.total[blockIdx.x]) *S.total[blockIdx.x] = carry_s;
-}
-
-__global__ void __launch_bounds__(SC_BLOCK) k_scan_down_set(ScanSet S, uint32_t n, const uint32_t* part,
-                                                             uint32_t stride) {
-  const uint32_t* in = S.in[blockIdx.y];
-  uint32_t* out = S.out[blockIdx.y];
-  uint32_t base = blockIdx.x * SC_TILE + threadIdx.x * SC_ITEMS;
-  uint32_t v[SC_ITEMS], s = 0;
-#pragma unroll
-  for (int i = 0; i < SC_ITEMS; ++i) {
-    v[i] = base + i < n ? in[base + i] : 0u;
-    s += v[i];
-  }
-  uint32_t ex = block_exclusive_scan(s, nullptr) + part[(size_t)blockIdx.y * stride + blockIdx.x];
-#pragma unroll
-  for (int i = 0; i < SC_ITEMS; ++i) {
-    if (base + i < n) out[base + i] = ex;
-    ex += v[i];
-  }
-}
-
-void launch_exclusive_scan_set(const ScanSet& S, int count, uint32_t n, uint32_t* part, cudaStream_t s) {
-  if (n == 0 || count <= 0) return;
-  const uint32_t nb = (n + SC_TILE - 1) / SC_TILE;
-  const uint32_t stride = scan_parts_needed(n);
-  k_scan_reduce_set<<<dim3(nb, (unsigned)count), SC_BLOCK, 0, s>>>(S, n, part, stride);
-  k_scan_top_set<<<(unsigned)count, 1024, 0, s>>>(S, part, nb, stride);
-  k_scan_down_set<<<dim3(nb, (unsigned)count), SC_BLOCK, 0, s>>>(S, n, part, stride);
-}
-
 uint32_t scan_parts_needed(uint32_t n) { return (n + SC_TILE - 1) / SC_TILE + 1; }
 uint32_t radix_hist_needed(uint32_t n) { return 256u * ((n + RS_TILE - 1) / RS_TILE) + 1; }
 

@@ -1029,12 +1029,46 @@ __device__ __forceinline__ bool sjkr_far_zero(const StepParams& P, const Law& L,
   return (rsum - d) + e < dc - 1e-5f * fabsf(dc);
 }
 
+// Exclusive prefix of v over the lanes of the warp, and the warp's total.
+// Every lane of the warp takes part.
+__device__ __forceinline__ uint32_t warp_exclusive(uint32_t v, uint32_t& total) {
+  const int lane = threadIdx.x & 31;
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+    if (lane >= o) x += y;
+  }
+  total = __shfl_sync(0xFFFFFFFFu, x, 31);
+  return x - v;
+}
+
+// v slots of the array behind a device counter for each lane of the warp,
+// contiguous in lane order, with one atomic per warp: returns this lane's
+// first slot. Every lane of the warp takes part.
+__device__ __forceinline__ uint32_t warp_reserve(uint32_t* ctr, uint32_t v) {
+  uint32_t total;
+  const uint32_t ex = warp_exclusive(v, total);
+  uint32_t base = 0;
+  if ((threadIdx.x & 31) == 0 && total) base = atomicAdd(ctr, total);
+  return __shfl_sync(0xFFFFFFFFu, base, 0) + ex;
+}
+
+// The contact pass's counters (records, evaluating records, network queue,
+// deferred pairs, wall queue) start every force pass at zero.
+constexpr int CTOT_WORDS = 8;
+
 // Pass 1 (FP32 and integer work only): the candidates of each particle, i.e.
 // list entries the FP32 pretest cannot rule out and that the reference's loop
-// visits from this end (visit counts from both ends recorded); counts all
-// candidates and the ones that evaluate their pair (the lower slot of a pair
-// seen from both ends, or the only end that sees it). The pretest is
-// symmetric, so a pair seen from both ends is a candidate at both.
+// visits from this end (visit counts from both ends recorded); marks the ones
+// that evaluate their pair (the lower slot of a pair seen from both ends, or
+// the only end that sees it). The pretest is symmetric, so a pair seen from
+// both ends is a candidate at both. Each warp then reserves, with one atomic
+// per counter, the result slots of its particles' records (coff) and their
+// places in the compact list of evaluating records (and the network queue):
+// where a record's result lands changes nothing in its value, and each
+// particle's results stay contiguous and in list order. The block size is a
+// multiple of 32 and every lane of a warp runs the same number of iterations.
 template <bool PHYS, bool HIST>
 __global__ void __launch_bounds__(256, 4) k_contact_filter(StepParams P) {
   Ctrl* C = P.ctrl;
@@ -1053,10 +1087,11 @@ __global__ void __launch_bounds__(256, 4) k_contact_filter(StepParams P) {
   const size_t plane = (size_t)P.n * P.cap;
   // slots in the rebuild-time order (tiles of 256 sorted by list length), so
   // a warp's lanes walk lists of similar length
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n; i += gridDim.x * blockDim.x) {
-    const int k = (int)P.aorder[i];
+  for (int i0 = blockIdx.x * blockDim.x; i0 < P.n; i0 += gridDim.x * blockDim.x) {
+    const int i = i0 + (int)threadIdx.x;
+    const int k = i < P.n ? (int)P.aorder[i] : -1;
     uint32_t nrec = 0, ncmp = 0, nnet = 0;
-    if (!(B.flags[k] & PF_DEAD)) {
+    if (k >= 0 && !(B.flags[k] & PF_DEAD)) {
       const unsigned long long ci = PHYS ? 0ull : (unsigned long long)__double_as_longlong(B.wc[k].w);
       // visits of a neighbour in the same reference cell (most pairs at a 1 m
       // cell): a constant, without the 27-cell walk of ref_visits
@@ -1105,28 +1140,20 @@ __global__ void __launch_bounds__(256, 4) k_contact_filter(StepParams P) {
         }
       }
     }
+    __syncwarp();
+    const uint32_t rb = warp_reserve(P.ctot, nrec);
+    uint32_t q = warp_reserve(P.ctot + 1, ncmp);
+    uint32_t qn = learn_any ? warp_reserve(P.ctot + 2, nnet) : 0u;
+    if (k < 0) continue;
     P.ccnt[k] = nrec;
-    P.ncomp[k] = ncmp;
-    if (learn_any) P.nnet[k] = nnet;
-  }
-}
-
-// Pass 2: the compact list of evaluating records, and the network queue (in
-// particle order, at the offsets of the scan of the per-particle counts).
-__global__ void __launch_bounds__(256) k_contact_index(StepParams P) {
-  if (P.ctrl->halt) return;
-  const bool learn = P.jkr_solver == 1 && P.nmodel == 3 && P.mlp != nullptr;
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    P.ctot[3] = 0u;  // deferred pairs of this step
-    P.ctot[4] = 0u;  // particles queued for k_accumulate_walls
-  }
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < P.n; k += gridDim.x * blockDim.x) {
-    const uint32_t n = P.ccnt[k];
-    uint32_t q = P.poff[k];
-    uint32_t qn = learn ? P.noff[k] : 0u;
+    P.coff[k] = rb;
+    if (ncmp == 0) continue;
+    // the evaluating records into the compact list (the queued ones into the
+    // network queue too), read back from the row this thread just wrote
     const size_t base = (size_t)k * P.cap;
-    for (uint32_t c = 0; c < n; ++c) {
-      const CRec r = P.crec[base + c];
+    const CRec* out = P.crec + base;
+    for (uint32_t c = 0; c < nrec; ++c) {
+      const CRec r = out[c];
       if (!(crec_vji(r.mv) > 0 && (uint32_t)k > r.j)) {
         if (r.mv & CREC_NET) P.jq[qn++] = make_uint2(q, (uint32_t)(base + c));
         P.clist[q++] = (uint32_t)(base + c);
@@ -1749,15 +1776,12 @@ static int launch_contact_path(const StepParams& P, cudaStream_t s) {
             ba = P.bs_accum > 0 ? P.bs_accum : 128, cap = P.grid_cap > 0 ? P.grid_cap : P.nsm * 64;
   const int g = shaped_grid((uint64_t)P.n, bf, cap);
   const bool hist = P.mode == 1 && P.tmodel != 0;
+  cudaMemsetAsync(P.ctot, 0, sizeof(uint32_t) * CTOT_WORDS, s);
   if (P.mode == 0) k_contact_filter<false, false><<<g, bf, 0, s>>>(P);
   else if (hist) k_contact_filter<true, true><<<g, bf, 0, s>>>(P);
   else k_contact_filter<true, false><<<g, bf, 0, s>>>(P);
-  // record offsets, evaluating-record offsets (and the network queue's) in one set of scans
   const bool learn = P.jkr_solver == 1 && P.nmodel == 3 && P.mlp != nullptr;
-  const ScanSet S{{P.ccnt, P.ncomp, P.nnet}, {P.coff, P.poff, P.noff}, {P.ctot, P.ctot + 1, P.ctot + 2}};
-  launch_exclusive_scan_set(S, learn ? 3 : 2, (uint32_t)P.n, P.cpart, s);
-  int launched = 7;
-  k_contact_index<<<grid_for(P.n, 256), 256, 0, s>>>(P);
+  int launched = 3;
   if (learn) {
     k_jkr_mlp<<<P.nsm * 4, 128, 0, s>>>(P);
     ++launched;

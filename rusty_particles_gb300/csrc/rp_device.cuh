@@ -132,15 +132,12 @@ struct StepParams {
   uint32_t* aorder; // slots in the order k_accumulate visits them (a permutation within tiles of 256)
   uint2* wq;        // (slot, wall candidates) of the particles with a wall candidate; length ctot[4]
   uint32_t* wcand;  // per slot, the first WALL_CAND_CAP triangles that passed the wall pretest
-  uint32_t* ncomp;  // records that evaluate their pair (each pair once)
-  uint32_t* coff;   // exclusive scan of ccnt: result offset of particle k
-  uint32_t* poff;   // exclusive scan of ncomp
+  uint32_t* coff;   // first result slot of particle k (its ccnt results are contiguous)
   uint32_t* clist;  // compact list of evaluating record slots
   uint32_t* ctot;   // [0] records, [1] evaluating records, [2] network queue, [3] deferred pairs, [4] wall queue
   uint32_t* jfb;    // evaluating indices deferred to the reference-Newton pass (null: no deferral)
   double* cres;     // per record: force (3) and torque (3) on the row's particle
   float* cresf;     // the same buffer as FP32 records (the mixed form: its pair forces are FP32 values)
-  uint32_t* cpart;  // scan partials
   int nmodel, tmodel, mode, prec;
   int periodic[3];
   int debug;
@@ -180,8 +177,6 @@ struct StepParams {
   float jdom_lo[4], jdom_hi[4];  // raw-feature range of the training set
   const MlpInfer* mlp;
   uint2* jq;        // network queue: (evaluating index, record slot); length ctot[2]
-  uint32_t* nnet;   // queued records per particle
-  uint32_t* noff;   // exclusive scan of nnet
   float* jguess;    // per evaluating index: predicted a/R* (NaN = outside the training range)
   // diagnostics
   double* dbgF;

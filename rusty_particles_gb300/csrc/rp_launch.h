@@ -33,14 +33,6 @@ struct RebuildBufs {
 void launch_exclusive_scan(const Ctrl* gate, const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* part,
                            uint32_t* total, cudaStream_t s);
 uint32_t scan_parts_needed(uint32_t n);
-// Up to three exclusive scans of n values each in one set of three launches;
-// part holds count * scan_parts_needed(n) entries; a null total is skipped.
-struct ScanSet {
-  const uint32_t* in[3];
-  uint32_t* out[3];
-  uint32_t* total[3];
-};
-void launch_exclusive_scan_set(const ScanSet& S, int count, uint32_t n, uint32_t* part, cudaStream_t s);
 uint32_t radix_hist_needed(uint32_t n);
 int launch_radix_sort(const Ctrl* gate, uint32_t* ka, uint32_t* va, uint32_t* kb, uint32_t* vb, uint32_t n, int bits,
                       uint32_t* hist, uint32_t* part, cudaStream_t s);
