@@ -1104,11 +1104,19 @@ __global__ void __launch_bounds__(256, 4) k_contact_filter(StepParams P) {
       const uint32_t cnt = B.ncnt[k];
       const uint32_t* row = B.nbr + (size_t)k * P.cap;
       CRec* out = P.crec + (size_t)k * P.cap;
+      // the next entry and its FP32 position are loaded while this one is
+      // tested (rows and positions are read-only during the pass)
+      uint32_t jn = cnt > 0 ? __ldg(row) : 0u;
+      float4 xn = cnt > 0 ? __ldg(B.xf + jn) : make_float4(0.f, 0.f, 0.f, 0.f);
       for (uint32_t m = 0; m < cnt; ++m) {
-        const uint32_t j = row[m];
+        const uint32_t j = jn;
+        const float4 xjf = xn;
+        if (m + 1 < cnt) {
+          jn = __ldg(row + m + 1);
+          xn = __ldg(B.xf + jn);
+        }
         const size_t hi = (size_t)k * P.cap + m;
         int vij = 0, vji = 0;
-        const float4 xjf = B.xf[j];
         if (!(P.pretest && pretest_far(P, xif, Xi, xjf, adh)) && !(zdrop && jkr_far_zero(P, lw.jkr_Cf, xif, Xi, xjf)) &&
             !(sdrop && sjkr_far_zero(P, lw, xif, Xi, xjf))) {
           if (PHYS) {
