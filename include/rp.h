@@ -107,6 +107,7 @@ typedef struct rp_stats {
 #define RP_STATUS_OVERLAP 1u    /* overlap > 20 % of the smaller radius (src/simulation.rs:361-370) */
 #define RP_STATUS_NAN_FORCE 2u  /* a non-finite particle force */
 #define RP_STATUS_NLIST_GROW 4u /* a neighbour list outgrew its capacity (recovered) */
+#define RP_STATUS_WALL_GROW 8u  /* the wall contact candidates outgrew their buffer (recovered) */
 
 /* --- lifecycle: Simulation.create (src/lib.rs:57, src/simulation.rs:62-91) */
 rp_sim* rp_create(double dt, const double min_xyz[3], const double max_xyz[3], size_t particle_capacity);

@@ -122,7 +122,8 @@ void Engine::free_device() {
   dfree(rb_.ka); dfree(rb_.va); dfree(rb_.kb); dfree(rb_.vb); dfree(rb_.hist); dfree(rb_.part);
   dfree(rb_.cstart); dfree(rb_.cend); dfree(kraw_);
   dfree(dbgF_); dfree(dbgT_); dfree(dbgMult_); dfree(ke_);
-  dfree(crec_); dfree(clist_); dfree(cres_); dfree(ccnt_); dfree(aorder_); dfree(wq_); dfree(wcand_); dfree(coff_);
+  dfree(crec_); dfree(clist_); dfree(cres_); dfree(ccnt_); dfree(aorder_); dfree(coff_);
+  dfree(warena_); dfree(wres_); dfree(wok_); dfree(woff_); dfree(wcnt_);
   dfree(ctot_);
   dfree(tri_d_); dfree(tstart_d_); dfree(titems_d_); dfree(glaw_d_); dfree(motions_d_);
   dfree(mlp_d_); dfree(jq_); dfree(jguess_); dfree(jfb_);
@@ -322,7 +323,9 @@ int Engine::alloc_slots(size_t n) {
   TRY(dalloc(&rb_.hist, hn));
   TRY(dalloc(&rb_.part, scan_parts_needed(std::max<uint32_t>(hn, (uint32_t)na)) + 16));
   TRY(dalloc(&dbgF_, 3 * na)); TRY(dalloc(&dbgT_, 3 * na));
-  TRY(dalloc(&aorder_, na)); TRY(dalloc(&wq_, na)); TRY(dalloc(&wcand_, na * WALL_CAND_CAP));
+  TRY(dalloc(&aorder_, na));
+  TRY(dalloc(&woff_, na)); TRY(dalloc(&wcnt_, na));
+  TRY(alloc_walls(std::max(wcap_, na / 2 + 65536)));
   TRY(dalloc(&ccnt_, na)); TRY(dalloc(&coff_, na));
   TRY(dalloc(&ctot_, 8));
   CK(cudaMemset(ctot_, 0, 8 * sizeof(uint32_t)));
@@ -333,6 +336,18 @@ int Engine::alloc_slots(size_t n) {
     dfree(bank_[b].hist);
   }
   dfree(dbgMult_);
+  return RP_OK;
+}
+
+// The wall candidate arena of the force pass (candidates, their results and
+// contact flags), room for `cap` candidates. A filter that finds it full
+// halts the step (HALT_WALLS) and recover_halt grows it.
+int Engine::alloc_walls(size_t cap) {
+  TRY(dalloc(&warena_, cap));
+  TRY(dalloc(&wres_, 6 * cap));
+  TRY(dalloc(&wok_, cap));
+  wcap_ = cap;
+  refresh_list_ptrs();
   return RP_OK;
 }
 
@@ -434,8 +449,12 @@ void Engine::refresh_list_ptrs() {
   P_.cresf = reinterpret_cast<float*>(cres_);
   P_.ccnt = ccnt_;
   P_.aorder = aorder_;
-  P_.wq = wq_;
-  P_.wcand = wcand_;
+  P_.warena = warena_;
+  P_.wres = wres_;
+  P_.wok = wok_;
+  P_.woff = woff_;
+  P_.wcnt = wcnt_;
+  P_.wcap = (uint32_t)wcap_;
   P_.coff = coff_;
   P_.ctot = ctot_;
 }
@@ -918,18 +937,26 @@ int Engine::finish_step_accounting() {
 }
 
 // A list outgrew its capacity during the rebuild of the step after
-// `steps_done` (that step's first half already ran): grow the lists, keeping
-// the current bank's rows for the history carry-over, and finish that step.
+// `steps_done`, or the wall candidates their arena during its contact filter
+// (that step's first half already ran): grow the lists (keeping the current
+// bank's rows for the history carry-over) or the arena, and finish that step.
 int Engine::recover_halt() {
   while (ctrl_h_->halt) {
-    int newcap = std::max<int>(cap_ + 8, (int)(ctrl_h_->max_count * 5 / 4 + 8));
-    TRY(alloc_lists(newcap, true));
+    if (ctrl_h_->halt & HALT_LISTS) {
+      int newcap = std::max<int>(cap_ + 8, (int)(ctrl_h_->max_count * 5 / 4 + 8));
+      TRY(alloc_lists(newcap, true));
+      tot_.status |= ST_NLIST_GROW;
+    }
+    if (ctrl_h_->halt & HALT_WALLS) {
+      TRY(alloc_walls(std::max<size_t>(wcap_ * 2, (size_t)ctrl_h_->wall_need * 5 / 4 + 65536)));
+      tot_.status |= ST_WALL_GROW;
+    }
     graph_dirty_ = true;
-    tot_.status |= ST_NLIST_GROW;
     int zero = 0;
     unsigned zu = 0;
     CK(cudaMemcpyAsync(&ctrl_->halt, &zero, sizeof(int), cudaMemcpyHostToDevice, stream_));
     CK(cudaMemcpyAsync(&ctrl_->max_count, &zu, sizeof(unsigned), cudaMemcpyHostToDevice, stream_));
+    CK(cudaMemcpyAsync(&ctrl_->wall_need, &zu, sizeof(unsigned), cudaMemcpyHostToDevice, stream_));
     CK(cudaStreamSynchronize(stream_));
     launches_ += launch_rebuild(P_, rb_, stream_);
     launches_ += launch_force(P_, stream_);

@@ -145,8 +145,11 @@ class Engine {
   CRec* crec_ = nullptr;
   uint32_t *ccnt_ = nullptr, *coff_ = nullptr, *clist_ = nullptr;
   uint32_t* aorder_ = nullptr;  // k_accumulate visiting order (set at every list rebuild)
-  uint2* wq_ = nullptr;         // wall queue of the accumulate pass
-  uint32_t* wcand_ = nullptr;   // wall candidates per slot
+  uint2* warena_ = nullptr;     // wall candidates of the force pass
+  double* wres_ = nullptr;      // their results
+  uint8_t* wok_ = nullptr;      // their contact flags
+  uint32_t *woff_ = nullptr, *wcnt_ = nullptr;
+  size_t wcap_ = 0;
   uint32_t *ctot_ = nullptr;
   double* cres_ = nullptr;
   void refresh_list_ptrs();
@@ -201,6 +204,7 @@ class Engine {
   int build_graph();
   void destroy_graph();
   int recover_halt();
+  int alloc_walls(size_t cap);
   int sync_ctrl();
   int finish_step_accounting();
 };

@@ -412,7 +412,7 @@ __global__ void k_build_nlist(StepParams P, const uint32_t* cstart, const uint32
         }
     B.ncnt[k] = cnt < (uint32_t)P.cap ? cnt : (uint32_t)P.cap;
     atomicMax(&P.ctrl->max_count, cnt);
-    if (cnt > (uint32_t)P.cap) atomicExch(&P.ctrl->halt, 1);
+    if (cnt > (uint32_t)P.cap) atomicOr(&P.ctrl->halt, HALT_LISTS);
   }
 }
 

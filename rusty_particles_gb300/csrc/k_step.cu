@@ -1090,7 +1090,9 @@ __global__ void __launch_bounds__(256, 4) k_contact_filter(StepParams P) {
   for (int i0 = blockIdx.x * blockDim.x; i0 < P.n; i0 += gridDim.x * blockDim.x) {
     const int i = i0 + (int)threadIdx.x;
     const int k = i < P.n ? (int)P.aorder[i] : -1;
-    uint32_t nrec = 0, ncmp = 0, nnet = 0;
+    uint32_t nrec = 0, ncmp = 0, nnet = 0, nw = 0, ts = 0, te = 0, gi = 0;
+    float4 xif = make_float4(0.f, 0.f, 0.f, 0.f);
+    float Xi = 0.f;
     if (k >= 0 && !(B.flags[k] & PF_DEAD)) {
       const unsigned long long ci = PHYS ? 0ull : (unsigned long long)__double_as_longlong(B.wc[k].w);
       // visits of a neighbour in the same reference cell (most pairs at a 1 m
@@ -1099,8 +1101,8 @@ __global__ void __launch_bounds__(256, 4) k_contact_filter(StepParams P) {
       const Law lw = law_of(P, B, k);  // pairs never cross groups (the lists exclude them)
       const bool adhesive = lw.gamma_pp > 0.0;
       const bool learn = learn_any && adhesive, zdrop = zdrop_any && adhesive;
-      const float4 xif = B.xf[k];
-      const float Xi = fmaxf(fmaxf(fabsf(xif.x), fabsf(xif.y)), fabsf(xif.z));
+      xif = B.xf[k];
+      Xi = fmaxf(fmaxf(fabsf(xif.x), fabsf(xif.y)), fabsf(xif.z));
       const uint32_t cnt = B.ncnt[k];
       const uint32_t* row = B.nbr + (size_t)k * P.cap;
       CRec* out = P.crec + (size_t)k * P.cap;
@@ -1147,14 +1149,36 @@ __global__ void __launch_bounds__(256, 4) k_contact_filter(StepParams P) {
           if (P.debug) P.dbgMult[hi] = 0;
         }
       }
+      // wall candidates: the triangles of its triangle-grid cell that pass
+      // the FP32 pretest, counted here and listed once the arena is reserved
+      if (P.ntri > 0 && tri_cell_range(P, xif, ts, te)) {
+        gi = P.ngroups > 1 ? B.grp[k] : 0u;
+        for (uint32_t t = ts; t < te; ++t) nw += wall_pretest(P.tri[P.titems[t]], gi, xif, Xi) ? 1u : 0u;
+      }
     }
     __syncwarp();
     const uint32_t rb = warp_reserve(P.ctot, nrec);
     uint32_t q = warp_reserve(P.ctot + 1, ncmp);
     uint32_t qn = learn_any ? warp_reserve(P.ctot + 2, nnet) : 0u;
+    const uint32_t wb = P.ntri > 0 ? warp_reserve(P.ctot + 4, nw) : 0u;
     if (k < 0) continue;
     P.ccnt[k] = nrec;
     P.coff[k] = rb;
+    if (P.ntri > 0) {
+      if (nw > 0 && wb + nw <= P.wcap) {  // in mesh order, as the reference visits them
+        uint2* dst = P.warena + wb;
+        uint32_t c = 0;
+        for (uint32_t t = ts; t < te && c < nw; ++t) {
+          const uint32_t id = P.titems[t];
+          if (wall_pretest(P.tri[id], gi, xif, Xi)) dst[c++] = make_uint2((uint32_t)k, id);
+        }
+      } else if (nw > 0) {  // the arena is full: the step halts and the host grows it
+        atomicMax(&C->wall_need, wb + nw);
+        atomicOr(&C->halt, HALT_WALLS);
+      }
+      P.wcnt[k] = nw;
+      P.woff[k] = wb;
+    }
     if (ncmp == 0) continue;
     // the evaluating records into the compact list (the queued ones into the
     // network queue too), read back from the row this thread just wrote
@@ -1335,17 +1359,40 @@ __device__ __forceinline__ bool contact_eval(const StepParams& P, const Bank& B,
   return false;
 }
 
+// A wall candidate of the filter: the FP64 sphere-triangle contact
+// (src/simulation.rs:464-523); its force and torque are kept for
+// k_accumulate, which adds them after the pair contacts in mesh order.
+__device__ __forceinline__ void wall_eval(const StepParams& P, const Bank& B, uint32_t w, bool& excess) {
+  const uint2 e = P.warena[w];
+  const int k = (int)e.x;
+  const D4 xi = B.xr[k], vi = B.vm[k], wi = B.wc[k];
+  V fc, tc;
+  const bool ok = wall_contact(P, law_of(P, B, k), P.tri[e.y], xyz(xi), xyz(vi), xyz(wi), xi.w, vi.w, fc, tc, excess);
+  if (ok) {
+    double2* o = reinterpret_cast<double2*>(P.wres + 6 * (size_t)w);
+    o[0] = make_double2(fc.x, fc.y);
+    o[1] = make_double2(fc.z, tc.x);
+    o[2] = make_double2(tc.y, tc.z);
+  }
+  P.wok[w] = ok ? 1 : 0;
+}
+
+// Pass 3: one thread per evaluating record, then one per wall candidate (the
+// few wall contacts spread over the whole grid with the pairs).
 template <bool PHYS, bool HIST, typename R>
 __global__ void __launch_bounds__(256) k_contact_force(StepParams P) {
   Ctrl* C = P.ctrl;
   if (C->halt) return;
   const Bank B = P.bank[C->bank];
   const uint32_t total = P.ctot[1];
+  const uint32_t items = total + (P.ntri > 0 ? min(P.ctot[4], P.wcap) : 0u);
   bool excess = false;
   uint32_t tally[6] = {0u, 0u, 0u, 0u, 0u, 0u};
   const int lane = threadIdx.x & 31;
-  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
-    const bool deferred = contact_eval<PHYS, HIST, R>(P, B, t, true, excess, tally);
+  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < items; t += gridDim.x * blockDim.x) {
+    bool deferred = false;
+    if (t < total) deferred = contact_eval<PHYS, HIST, R>(P, B, t, true, excess, tally);
+    else wall_eval(P, B, t - total, excess);
     // append the deferred pairs with one atomic per warp
     const unsigned act = __activemask();
     const unsigned bal = __ballot_sync(act, deferred);
@@ -1382,18 +1429,15 @@ __global__ void __launch_bounds__(128) k_contact_deferred(StepParams P) {
   if (excess) C->overlap_flag = 1;
 }
 
-// Pass 4: per particle, the contact results in list order, the walls, then
-// a = g + F/m and tau = T (src/simulation.rs:265-271, 532-536), in two
-// kernels. k_accumulate (few registers, many warps in flight for the loads)
-// sums the contact results of every particle and finishes those whose
-// triangle-grid cell lists no triangle; the others are queued with their
-// partial F and T, and k_accumulate_walls adds their wall contacts: FP32
-// pretests per particle, then the block's (particle, triangle) candidates
-// evaluated densely, one per thread per round, with results in shared
-// memory; each particle adds its own in mesh order, so F and T are the same
-// sums as one thread walking its triangles. k_accumulate takes the slots in
-// the order P.aorder, set at each list rebuild, so that a warp's lanes run
-// loops of similar length; no order changes a result.
+// Pass 4: per particle, the contact results in list order, then the wall
+// contacts in mesh order, then a = g + F/m and tau = T
+// (src/simulation.rs:265-271, 464-536). The wall candidates were listed by
+// the filter (FP32 pretests against the triangles of the particle's
+// triangle-grid cell) and evaluated by the pair kernel, one thread each, so
+// F and T are the same sums as one thread walking its triangles.
+// k_accumulate takes the slots in the order P.aorder, set at each list
+// rebuild, so that a warp's lanes run loops of similar length; no order
+// changes a result.
 constexpr uint32_t ACC_BINS = 128;
 constexpr uint32_t ACC_TILE = 256;
 
@@ -1508,7 +1552,6 @@ __global__ void __launch_bounds__(256) k_accumulate(StepParams P) {
   Ctrl* C = P.ctrl;
   if (C->halt) return;
   const Bank B = P.bank[C->bank];
-  const int lane = threadIdx.x & 31;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n; i += gridDim.x * blockDim.x) {
     const int k = (int)P.aorder[i];
     if (B.flags[k] & PF_DEAD) continue;
@@ -1529,130 +1572,19 @@ __global__ void __launch_bounds__(256) k_accumulate(StepParams P) {
         T = T + vmk(r1.y, r2.x, r2.y);
       }
     }
-    // wall pretests: the first WALL_CAND_CAP triangles that pass are kept
-    // for k_accumulate_walls (a count above the cap says there are more)
-    uint32_t nc = 0;
+    // the wall contacts after the pair contacts, in mesh order
     if (P.ntri > 0) {
-      const float4 xf = B.xf[k];
-      uint32_t s, e;
-      if (tri_cell_range(P, xf, s, e) && e > s) {
-        const float xmag = fmaxf(fmaxf(fabsf(xf.x), fabsf(xf.y)), fabsf(xf.z));
-        const uint32_t gi = P.ngroups > 1 ? B.grp[k] : 0u;
-        uint32_t* out = P.wcand + (size_t)k * WALL_CAND_CAP;
-        for (uint32_t t = s; t < e; ++t) {
-          const uint32_t id = P.titems[t];
-          if (!wall_pretest(P.tri[id], gi, xf, xmag)) continue;
-          if (nc == WALL_CAND_CAP) {
-            ++nc;
-            break;
-          }
-          out[nc++] = id;
-        }
-      }
-    }
-    const bool walls = nc > 0;
-    // queue the particles with wall candidates, one atomic per warp
-    const unsigned act = __activemask();
-    const unsigned bal = __ballot_sync(act, walls);
-    if (bal) {
-      const int leader = __ffs(bal) - 1;
-      uint32_t q = 0;
-      if (lane == leader) q = atomicAdd(P.ctot + 4, (uint32_t)__popc(bal));
-      q = __shfl_sync(act, q, leader);
-      if (walls) P.wq[q + (uint32_t)__popc(bal & ((1u << lane) - 1u))] = make_uint2((uint32_t)k, nc);
-    }
-    if (walls) {  // partial sums, completed by k_accumulate_walls
-      B.acc[k] = D4{F.x, F.y, F.z, 0.0};
-      B.tq[k] = D4{T.x, T.y, T.z, 0.0};
-    } else {
-      finish_particle(P, B, C, k, F, T);
-    }
-  }
-}
-
-__global__ void __launch_bounds__(256) k_accumulate_walls(StepParams P) {
-  Ctrl* C = P.ctrl;
-  if (C->halt) return;
-  const Bank B = P.bank[C->bank];
-  const uint32_t total = P.ctot[4];
-  __shared__ uint32_t kslot[256];  // the slot each thread of the tile took
-  __shared__ uint32_t woff[257];   // per-thread candidate offsets, then the block total
-  __shared__ uint32_t wsum[8];
-  __shared__ double wres[6][256];  // one round of dense results (force, torque)
-  __shared__ uint8_t wok[256];
-  bool excess = false;
-  for (uint32_t base = blockIdx.x * blockDim.x; base < total; base += gridDim.x * blockDim.x) {
-    const uint32_t i = base + threadIdx.x;
-    const bool live = i < total;
-    const uint2 qe = live ? P.wq[i] : make_uint2(0u, 0u);
-    const int k = (int)qe.x;
-    const uint32_t nc = min(qe.y, WALL_CAND_CAP);
-    V F = vmk(0.0, 0.0, 0.0), T = vmk(0.0, 0.0, 0.0);
-    if (live) {
-      F = xyz(B.acc[k]);
-      T = xyz(B.tq[k]);
-    }
-    kslot[threadIdx.x] = (uint32_t)k;
-    const uint32_t off = block_excl_scan(nc, wsum, &woff[blockDim.x]);
-    woff[threadIdx.x] = off;
-    __syncthreads();
-    const uint32_t W = woff[blockDim.x];
-    for (uint32_t r0 = 0; r0 < W; r0 += blockDim.x) {
-      const uint32_t w = r0 + threadIdx.x;
-      if (w < W) {
-        uint32_t lo = 0, hi = blockDim.x - 1;  // the last thread whose offset is <= w owns it
-        while (lo < hi) {
-          const uint32_t mid = (lo + hi + 1) >> 1;
-          if (woff[mid] <= w) lo = mid;
-          else hi = mid - 1;
-        }
-        const int ko = (int)kslot[lo];
-        const uint32_t id = P.wcand[(size_t)ko * WALL_CAND_CAP + (w - woff[lo])];
-        const D4 xo = B.xr[ko], vo = B.vm[ko], wo = B.wc[ko];
-        V fc, tc;
-        const bool ok = wall_contact(P, law_of(P, B, ko), P.tri[id], xyz(xo), xyz(vo), xyz(wo), xo.w, vo.w, fc, tc,
-                                     excess);
-        wok[threadIdx.x] = ok ? 1 : 0;
-        if (ok) {
-          wres[0][threadIdx.x] = fc.x; wres[1][threadIdx.x] = fc.y; wres[2][threadIdx.x] = fc.z;
-          wres[3][threadIdx.x] = tc.x; wres[4][threadIdx.x] = tc.y; wres[5][threadIdx.x] = tc.z;
-        }
-      }
-      __syncthreads();
-      const uint32_t a = max(off, r0), b = min(off + nc, r0 + blockDim.x);
-      for (uint32_t q = a; q < b; ++q) {
-        const uint32_t sl = q - r0;
-        if (wok[sl]) {
-          F = F + vmk(wres[0][sl], wres[1][sl], wres[2][sl]);
-          T = T + vmk(wres[3][sl], wres[4][sl], wres[5][sl]);
-        }
-      }
-      __syncthreads();
-    }
-    if (!live) continue;
-    if (qe.y > WALL_CAND_CAP) {  // candidates past the cap, inline, still in mesh order
-      const float4 xf = B.xf[k];
-      uint32_t s = 0, e = 0;
-      tri_cell_range(P, xf, s, e);
-      const float xmag = fmaxf(fmaxf(fabsf(xf.x), fabsf(xf.y)), fabsf(xf.z));
-      const uint32_t gi = P.ngroups > 1 ? B.grp[k] : 0u;
-      const D4 xi4 = B.xr[k], vi4 = B.vm[k], wi4 = B.wc[k];
-      const Law L = law_of(P, B, k);
-      uint32_t seen = 0;
-      for (uint32_t t = s; t < e; ++t) {
-        const TriRec& tr = P.tri[P.titems[t]];
-        if (!wall_pretest(tr, gi, xf, xmag)) continue;
-        if (seen++ < WALL_CAND_CAP) continue;  // evaluated in the dense rounds
-        V fc, tc;
-        if (wall_contact(P, L, tr, xyz(xi4), xyz(vi4), xyz(wi4), xi4.w, vi4.w, fc, tc, excess)) {
-          F = F + fc;
-          T = T + tc;
-        }
+      const uint32_t wn = P.wcnt[k], wo = P.woff[k];
+      for (uint32_t c = 0; c < wn; ++c) {
+        if (!P.wok[wo + c]) continue;
+        const double2* r = reinterpret_cast<const double2*>(P.wres + 6 * (size_t)(wo + c));
+        const double2 r0 = r[0], r1 = r[1], r2 = r[2];
+        F = F + vmk(r0.x, r0.y, r1.x);
+        T = T + vmk(r1.y, r2.x, r2.y);
       }
     }
     finish_particle(P, B, C, k, F, T);
   }
-  if (excess) C->overlap_flag = 1;
 }
 
 __global__ void k_clear_pending(StepParams P) {
@@ -1808,10 +1740,6 @@ static int launch_contact_path(const StepParams& P, cudaStream_t s) {
   }
   if (P.prec == 1) k_accumulate<true><<<shaped_grid((uint64_t)P.n, ba, cap), ba, 0, s>>>(P);
   else k_accumulate<false><<<shaped_grid((uint64_t)P.n, ba, cap), ba, 0, s>>>(P);
-  if (P.ntri > 0) {  // over the queue k_accumulate filled; its length is only known on the device
-    k_accumulate_walls<<<shaped_grid((uint64_t)P.n, 128, P.nsm * 16), 128, 0, s>>>(P);
-    ++launched;
-  }
   return launched;
 }
 

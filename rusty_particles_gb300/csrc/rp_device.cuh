@@ -21,13 +21,13 @@ struct alignas(32) D4 {
 
 enum : uint32_t { PF_FIXED = 1u, PF_DEAD = 2u };
 
-enum : unsigned { ST_OVERLAP = 1u, ST_NAN = 2u, ST_NLIST_GROW = 4u };
+enum : unsigned { ST_OVERLAP = 1u, ST_NAN = 2u, ST_NLIST_GROW = 4u, ST_WALL_GROW = 8u };
 
 // Device control block: written by kernels, read by the host after a chunk.
 struct Ctrl {
   int bank;                       // bank holding the current state
   int rebuild;                    // rebuild requested for the current step
-  int halt;                       // set when a list outgrew its capacity; later kernels of the chunk no-op
+  int halt;                       // HALT_* bits: a buffer outgrew its capacity; later kernels of the chunk no-op
   int overlap_flag;               // overlap > 20 % seen in the current step
   unsigned int status;            // sticky ST_* bits
   unsigned int max_count;         // longest neighbour list seen by the last build
@@ -36,7 +36,7 @@ struct Ctrl {
   unsigned long long rebuilds;    // completed list rebuilds
   unsigned long long overlap_steps;
   int pending;                    // the last completed step still owes its second half kick
-  int pad_;
+  unsigned int wall_need;         // wall candidates a halted filter wanted room for
   unsigned long long target;      // device step loop: run while steps_done < target
   unsigned long long iters;       // device step loop iterations (bounded by target + 4)
   // learned JKR tallies (pair evaluations): network/certified-solver results
@@ -63,7 +63,10 @@ struct Law {
   float jkr_Cf, pad_;
 };
 constexpr uint32_t GROUP_ALL = 0xFFFFFFFFu;
-constexpr uint32_t WALL_CAND_CAP = 8;  // wall candidates held per particle between the accumulate kernels
+// Ctrl::halt bits: a neighbour list outgrew its capacity (list rebuild), the
+// wall candidates outgrew their arena (contact filter)
+constexpr int HALT_LISTS = 1;
+constexpr int HALT_WALLS = 2;
 
 // A rigid surface velocity V + W x (p - C) of a set of triangles whose geometry
 // stays put (a surface of revolution turning about its own axis, a belt). The
@@ -130,8 +133,12 @@ struct StepParams {
   CRec* crec;       // n*cap records, row k at k*cap
   uint32_t* ccnt;   // records per particle
   uint32_t* aorder; // slots in the order k_accumulate visits them (a permutation within tiles of 256)
-  uint2* wq;        // (slot, wall candidates) of the particles with a wall candidate; length ctot[4]
-  uint32_t* wcand;  // per slot, the first WALL_CAND_CAP triangles that passed the wall pretest
+  uint2* warena;    // wall candidates (slot, triangle); a particle's at woff, in mesh order; min(ctot[4], wcap)
+  double* wres;     // per wall candidate: force (3) and torque (3) on the particle
+  uint8_t* wok;     // per wall candidate: 1 when the sphere touches the triangle
+  uint32_t* woff;   // first wall candidate of slot k
+  uint32_t* wcnt;   // wall candidates of slot k
+  uint32_t wcap;    // wall candidate capacity
   uint32_t* coff;   // first result slot of particle k (its ccnt results are contiguous)
   uint32_t* clist;  // compact list of evaluating record slots
   uint32_t* ctot;   // [0] records, [1] evaluating records, [2] network queue, [3] deferred pairs, [4] wall queue

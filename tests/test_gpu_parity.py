@@ -183,6 +183,39 @@ def test_one_step_fine_floor_many_wall_contacts(rp, oracle_mod):
     assert np.count_nonzero(Fo[:, 1] > 0) == k // 2
 
 
+def test_wall_candidates_outgrow_their_buffer(rp, oracle_mod):
+    # 360 spheres sunk 4 mm into a floor of 1 mm triangles: ~200 wall
+    # candidates each, more than the buffer a 360-particle simulation starts
+    # with (one per two slots plus 65,536), so the step halts, the buffer
+    # grows and the step runs again; the result is the oracle's
+    lo, hi = (-0.15, -0.05, -0.15), (0.15, 0.1, 0.15)
+    m = 260
+    xs = np.linspace(-0.13, 0.13, m + 1)
+    X0, Z0 = np.meshgrid(xs[:-1], xs[:-1], indexing="ij")
+    X1, Z1 = np.meshgrid(xs[1:], xs[1:], indexing="ij")
+    a = np.stack([X0, np.zeros_like(X0), Z0], -1).reshape(-1, 3)
+    b = np.stack([X1, np.zeros_like(X0), Z0], -1).reshape(-1, 3)
+    c = np.stack([X0, np.zeros_like(X0), Z1], -1).reshape(-1, 3)
+    d = np.stack([X1, np.zeros_like(X0), Z1], -1).reshape(-1, 3)
+    v = np.concatenate([np.concatenate([a, c, b], 1), np.concatenate([b, c, d], 1)]).astype(np.float32)
+    v = v.astype(np.float64)
+    n = np.tile([0.0, 1.0, 0.0], (len(v), 1))
+    rng = np.random.default_rng(43)
+    g = np.stack(np.meshgrid(np.arange(18), np.arange(20), indexing="ij"), -1).reshape(-1, 2)
+    k = len(g)
+    r = np.full(k, 0.006)
+    x = np.stack([-0.1105 + g[:, 0] * 0.013, 0.002 + rng.uniform(0.0, 1e-4, k), -0.1235 + g[:, 1] * 0.013], 1)
+    st = {"position": x, "radius": r, "mass": 2500.0 * 4.0 / 3.0 * np.pi * r ** 3,
+          "velocity": rng.normal(0, 0.05, (k, 3)), "angular_velocity": rng.normal(0, 1.0, (k, 3)),
+          "acceleration": np.zeros((k, 3)), "torque": np.zeros((k, 3)), "fixed": np.zeros(k, np.uint8)}
+    o, g = one_step(rp, oracle_mod, st, 1, 0, lo, hi, tris=(v, n), cell=0.02,
+                    wall=(1e8, 0.25, 7800.0, 0.3, 0.6, 0.0))
+    compare_step(o, g)
+    assert g.stats()["status_bits"] & 8  # the candidate buffer grew
+    Fo, _ = o.last_forces()
+    assert np.all(Fo[:, 1] > 0)
+
+
 def test_walls_across_list_rebuilds(rp, oracle_mod):
     # spheres sliding at 0.5 m/s over a floor of 4 mm triangles with a small
     # Verlet skin: the lists are rebuilt every few steps while the wall
