@@ -802,8 +802,8 @@ def roofline_of(sim, wl, n_now, prof_steps):
     achieved = alg_bytes / (force_ms / 1e3) / 1e9
     return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": None,
-            "kernel": ("force pass (k_contact_filter, scans, k_contact_index, k_contact_force, k_accumulate, "
-                       "k_accumulate_walls)"),
+            "kernel": ("force pass (k_contact_filter with the wall pretests, k_contact_force with the wall "
+                       "contacts, k_accumulate)"),
             "avg_launch_ms": force_ms, "force_share_of_step": force_ms / step_ms if step_ms > 0 else None,
             "algorithmic_bytes_per_launch": alg_bytes, "peak_source": peak_kind}
 

@@ -542,7 +542,9 @@ int Engine::build_params() {
     P.pretest = ok ? 1 : 0;
     P.lmax = (float)lm;
   }
-  double h = 2.0 * rmax * adh + skin;
+  // fine cells at least the largest list radius, with a relative 1e-7 to
+  // spare for the rounding of the cell lookup (fine_cell)
+  double h = (2.0 * rmax * adh + skin) * (1.0 + 1e-7);
   if (!(h > 0.0)) h = 1.0;
   const uint64_t max_cells = std::max<uint64_t>(4ull * (uint64_t)n_ + (1ull << 16), 1ull << 20);
   for (int iter = 0; iter < 64; ++iter) {
@@ -561,6 +563,17 @@ int Engine::build_params() {
     if (tot <= max_cells) break;
     h *= 1.25;
   }
+  double xb = 0.0;
+  for (int k = 0; k < 3; ++k) {
+    P.finv[k] = 1.0 / P.fcell[k];
+    P.binv[k] = P.bsize[k] > 0.0 ? 1.0 / P.bsize[k] : 0.0;
+    P.fcellf[k] = (float)P.fcell[k];
+    P.binvf[k] = (float)P.binv[k];
+    // live particles lie within 1.0 of the box (src/simulation.rs:199-219)
+    xb = std::max(xb, std::max(std::fabs(bmin[k]), std::fabs(bmax[k])) + 1.0);
+  }
+  P.rmaxf = (float)rmax;
+  P.xbound = (float)xb;
   P.fncells = (uint32_t)((uint64_t)P.fdims[0] * P.fdims[1] * P.fdims[2]);
   rb_.key_bits = bits_for(P.fncells);
   rb_.carry_history = (mode == RP_MODE_PHYSICAL && tmodel != RP_TANGENTIAL_COULOMB) ? 1 : 0;

@@ -317,6 +317,8 @@ __global__ void k_reorder(StepParams P, const uint32_t* perm) {
 // keeps every other particle within (cutoff + skin), tested in FP32 on the
 // FP64 difference with a small relative margin, so the list is a superset of
 // every pair the exact FP64 cutoff test can accept before the next rebuild.
+// A neighbouring cell farther from the particle than its largest list radius
+// (the largest radius as partner) holds no list entry and is skipped.
 // Physical mode carries each pair's tangential spring over from the old list.
 __global__ void k_build_nlist(StepParams P, const uint32_t* cstart, const uint32_t* cend, const uint32_t* perm,
                               int carry_history) {
@@ -342,21 +344,43 @@ __global__ void k_build_nlist(StepParams P, const uint32_t* cstart, const uint32
     c[0] = (int)(cl % (uint32_t)P.fdims[0]);
     c[1] = (int)((cl / (uint32_t)P.fdims[0]) % (uint32_t)P.fdims[1]);
     c[2] = (int)(cl / ((uint32_t)P.fdims[0] * (uint32_t)P.fdims[1]));
+    // the largest list radius of this particle (any partner: a partner within
+    // reach has coordinates below Xi + 2 rb, or within the box bound when it
+    // is a periodic image) plus the rounding of an FP32 distance again,
+    // grown by 1e-4; the cell gaps keep a thousandth of a cell for the
+    // rounding of the lookup
+    const float rb = (ri + P.rmaxf) * adh + skin;
+    const float Xe = fmaxf(Xi + 2.0f * rb, P.xbound);
+    const float rlm = (rb * P.list_scale + 5e-7f * (2.0f * Xe + P.lmax + rb)) * 1.0001f;
+    const double pq[3] = {xi.x, xi.y, xi.z};
     int off[3][3], no[3];
+    float gap[3][3];  // distance from the particle to each listed cell's slab (0: its own)
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
       no[a] = 0;
+      // position within its cell along the axis (the wrap as in fine_cell)
+      double q = pq[a] - P.fmin[a];
+      if (P.periodic[a]) q = q - floor(q * P.binv[a]) * P.bsize[a];
+      const float u = (float)(q - (double)c[a] * P.fcell[a]);
+      const float slack = 1e-3f * P.fcellf[a];
       if (P.fdims[a] >= 3) {
         for (int d = -1; d <= 1; ++d) {
-          int q = c[a] + d;
+          int qq = c[a] + d;
           if (P.periodic[a]) {
-            if (q < 0) q += P.fdims[a];
-            else if (q >= P.fdims[a]) q -= P.fdims[a];
+            if (qq < 0) qq += P.fdims[a];
+            else if (qq >= P.fdims[a]) qq -= P.fdims[a];
           }
-          if (q >= 0 && q < P.fdims[a]) off[a][no[a]++] = q;
+          if (qq >= 0 && qq < P.fdims[a]) {
+            const float g = d < 0 ? u : (d > 0 ? P.fcellf[a] - u : 0.0f);
+            gap[a][no[a]] = fmaxf(g - slack, 0.0f);
+            off[a][no[a]++] = qq;
+          }
         }
       } else {
-        for (int q = 0; q < P.fdims[a]; ++q) off[a][no[a]++] = q;
+        for (int qq = 0; qq < P.fdims[a]; ++qq) {
+          gap[a][no[a]] = 0.0f;
+          off[a][no[a]++] = qq;
+        }
       }
     }
     uint32_t cnt = 0;
@@ -367,6 +391,7 @@ __global__ void k_build_nlist(StepParams P, const uint32_t* cstart, const uint32
     for (int zz = 0; zz < no[2]; ++zz)
       for (int yy = 0; yy < no[1]; ++yy)
         for (int xx = 0; xx < no[0]; ++xx) {
+          if (gap[0][xx] * gap[0][xx] + gap[1][yy] * gap[1][yy] + gap[2][zz] * gap[2][zz] > rlm * rlm) continue;
           uint32_t cell = (uint32_t)off[0][xx] + (uint32_t)P.fdims[0] * ((uint32_t)off[1][yy] + (uint32_t)P.fdims[1] * (uint32_t)off[2][zz]);
           uint32_t s = cstart[cell];
           if (s == EMPTY) continue;
@@ -379,9 +404,10 @@ __global__ void k_build_nlist(StepParams P, const uint32_t* cstart, const uint32
             // 2.5e-7 (2X + L) + a relative 1e-5 keeps the list a superset
             const float4 xj = B.xf[j];
             float fx = xif.x - xj.x, fy = xif.y - xj.y, fz = xif.z - xj.z;
-            if (P.periodic[0]) fx -= P.bsizef[0] * rintf(fx / P.bsizef[0]);
-            if (P.periodic[1]) fy -= P.bsizef[1] * rintf(fy / P.bsizef[1]);
-            if (P.periodic[2]) fz -= P.bsizef[2] * rintf(fz / P.bsizef[2]);
+            // minimum image; where |f| < 0.49 L the image is the pair itself
+            if (P.periodic[0] && fabsf(fx * P.binvf[0]) > 0.49f) fx -= P.bsizef[0] * rintf(fx / P.bsizef[0]);
+            if (P.periodic[1] && fabsf(fy * P.binvf[1]) > 0.49f) fy -= P.bsizef[1] * rintf(fy / P.bsizef[1]);
+            if (P.periodic[2] && fabsf(fz * P.binvf[2]) > 0.49f) fz -= P.bsizef[2] * rintf(fz / P.bsizef[2]);
             float d2 = fx * fx + fy * fy + fz * fz;
             const float X = fmaxf(Xi, fmaxf(fmaxf(fabsf(xj.x), fabsf(xj.y)), fabsf(xj.z)));
             float rl = (ri + xj.w) * adh + skin;

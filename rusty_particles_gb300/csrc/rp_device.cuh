@@ -163,6 +163,10 @@ struct StepParams {
   int same_cell_visits;  // ref_visits(c, c) for a cell c inside the grid (3 per periodic axis of one cell, else 1)
   // fine grid (neighbour search)
   double fmin[3], fcell[3];
+  double finv[3], binv[3];  // 1 / fcell, 1 / bsize
+  float fcellf[3], binvf[3];
+  float rmaxf;              // largest radius (culls the cells of the list search)
+  float xbound;             // largest |box bound| + 1 (rounding margins of periodic images)
   int fdims[3];
   uint32_t fncells;
   double skin;
@@ -298,7 +302,10 @@ __device__ __forceinline__ bool ref_inside(const StepParams& P, unsigned long lo
   return true;
 }
 
-// Fine-grid cell of a position: periodic axes wrap, open axes clamp.
+// Fine-grid cell of a position: periodic axes wrap, open axes clamp. The
+// quotients are products with the reciprocals (a few ulps off the exact
+// ones); the cells are larger than the list radius by a relative 1e-7, so two
+// particles within the list radius still land in neighbouring cells.
 __device__ __forceinline__ uint32_t fine_cell(const StepParams& P, double x, double y, double z) {
   double p[3] = {x, y, z};
   int c[3];
@@ -307,9 +314,9 @@ __device__ __forceinline__ uint32_t fine_cell(const StepParams& P, double x, dou
     double q = p[k] - P.fmin[k];
     if (P.periodic[k]) {
       double L = P.bsize[k];
-      q = q - floor(q / L) * L;
+      q = q - floor(q * P.binv[k]) * L;
     }
-    double f = floor(q / P.fcell[k]);
+    double f = floor(q * P.finv[k]);
     int ck = (f != f) ? 0 : (f < 0.0 ? 0 : (f >= (double)P.fdims[k] ? P.fdims[k] - 1 : (int)f));
     c[k] = ck;
   }
