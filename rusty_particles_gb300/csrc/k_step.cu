@@ -1440,6 +1440,7 @@ __global__ void __launch_bounds__(128) k_contact_deferred(StepParams P) {
 // changes a result.
 constexpr uint32_t ACC_BINS = 128;
 constexpr uint32_t ACC_TILE = 256;
+constexpr uint32_t ACC_SORT_BINS = 32;  // record counts up to 31 (more share the last bin)
 
 __device__ __forceinline__ bool tri_cell_nonempty(const StepParams& P, float4 xf) {
   uint32_t s, e;
@@ -1552,18 +1553,56 @@ __global__ void __launch_bounds__(256) k_accumulate(StepParams P) {
   Ctrl* C = P.ctrl;
   if (C->halt) return;
   const Bank B = P.bank[C->bank];
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n; i += gridDim.x * blockDim.x) {
-    const int k = (int)P.aorder[i];
-    if (B.flags[k] & PF_DEAD) continue;
+  // Each block takes a tile of blockDim.x slots (in aorder) and deals them
+  // to its threads by their record and wall counts (a counting sort in shared
+  // memory), so the lanes of a warp run sum loops of about the same length:
+  // a partly filled FP64 warp instruction costs the pipe as much as a full one.
+  __shared__ uint32_t bins[ACC_SORT_BINS];
+  __shared__ int dealt[256];
+  for (int base = blockIdx.x * blockDim.x; base < P.n; base += gridDim.x * blockDim.x) {
+    const int i = base + (int)threadIdx.x;
+    int k = -1;
+    uint32_t key = 0;
+    if (i < P.n) {
+      k = (int)P.aorder[i];
+      if (B.flags[k] & PF_DEAD) k = -1;
+      else key = min(P.ccnt[k] + (P.ntri > 0 ? P.wcnt[k] : 0u), ACC_SORT_BINS - 1);
+    }
+    for (uint32_t b = threadIdx.x; b < ACC_SORT_BINS; b += blockDim.x) bins[b] = 0;
+    __syncthreads();
+    const uint32_t rank = atomicAdd(&bins[key], 1u);
+    __syncthreads();
+    if (threadIdx.x < 32) {  // exclusive scan of the bins, one per lane
+      const uint32_t c0 = bins[threadIdx.x];
+      uint32_t incl = c0;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (threadIdx.x >= (uint32_t)o) incl += t;
+      }
+      bins[threadIdx.x] = incl - c0;
+    }
+    __syncthreads();
+    dealt[bins[key] + rank] = k;
+    __syncthreads();
+    k = dealt[threadIdx.x];
+    __syncthreads();
+    if (k < 0) continue;
     V F = vmk(0.0, 0.0, 0.0), T = vmk(0.0, 0.0, 0.0);
     const uint32_t n = P.ccnt[k];
     if (F32REC) {
+      // the mixed form's FP32 pair forces summed in FP32 (in list order, from
+      // zero; the rounding adds at most (n - 1) 2^-24 of the sum of the
+      // magnitudes), then widened exactly
       const float2* res = reinterpret_cast<const float2*>(P.cresf + 6 * (size_t)P.coff[k]);
+      float fx = 0.0f, fy = 0.0f, fz = 0.0f, tx = 0.0f, ty = 0.0f, tz = 0.0f;
       for (uint32_t c = 0; c < n; ++c) {
         const float2 r0 = res[3 * c], r1 = res[3 * c + 1], r2 = res[3 * c + 2];
-        F = F + vmk(f2d_exact(r0.x), f2d_exact(r0.y), f2d_exact(r1.x));
-        T = T + vmk(f2d_exact(r1.y), f2d_exact(r2.x), f2d_exact(r2.y));
+        fx = fx + r0.x; fy = fy + r0.y; fz = fz + r1.x;
+        tx = tx + r1.y; ty = ty + r2.x; tz = tz + r2.y;
       }
+      F = vmk(f2d_exact(fx), f2d_exact(fy), f2d_exact(fz));
+      T = vmk(f2d_exact(tx), f2d_exact(ty), f2d_exact(tz));
     } else {
       const double2* res = reinterpret_cast<const double2*>(P.cres + 6 * (size_t)P.coff[k]);
       for (uint32_t c = 0; c < n; ++c) {
@@ -1572,7 +1611,7 @@ __global__ void __launch_bounds__(256) k_accumulate(StepParams P) {
         T = T + vmk(r1.y, r2.x, r2.y);
       }
     }
-    // the wall contacts after the pair contacts, in mesh order
+    // the wall contacts (FP64 in both forms) after the pair contacts, in mesh order
     if (P.ntri > 0) {
       const uint32_t wn = P.wcnt[k], wo = P.woff[k];
       for (uint32_t c = 0; c < wn; ++c) {
