@@ -618,6 +618,7 @@ int Engine::build_triangle_grid(double rmax) {
     P_.tri = nullptr;
     P_.tstart = nullptr;
     P_.titems = nullptr;
+    P_.wall_far_ok = 0;
     return RP_OK;
   }
   if (T > (size_t)0x3FFFFFF) {
@@ -764,6 +765,12 @@ int Engine::build_triangle_grid(double rmax) {
   }
   P_.tcell = cell;
   P_.tinvf = (float)(1.0 / cell);
+  // PF_WALLFAR needs a particle to stay among the 27 cells around its cell at
+  // the last rebuild, i.e. half the skin (the most it moves) below a cell
+  P_.wall_far_ok = (0.5 * P_.skin * 1.01 < cell) ? 1 : 0;
+  double bmag = 0.0;
+  for (int k = 0; k < 3; ++k) bmag = std::max(bmag, std::max(std::fabs(P_.bmin[k]), std::fabs(P_.bmax[k])));
+  P_.wall_far_gap = (float)(0.5 * P_.skin * 1.01 + 1e-6 * (1.0 + bmag));
   tgrid_built_ = true;
   return RP_OK;
 }

@@ -1093,7 +1093,8 @@ __global__ void __launch_bounds__(256, 4) k_contact_filter(StepParams P) {
     uint32_t nrec = 0, ncmp = 0, nnet = 0, nw = 0, ts = 0, te = 0, gi = 0;
     float4 xif = make_float4(0.f, 0.f, 0.f, 0.f);
     float Xi = 0.f;
-    if (k >= 0 && !(B.flags[k] & PF_DEAD)) {
+    const uint32_t flk = k >= 0 ? B.flags[k] : PF_DEAD;
+    if (!(flk & PF_DEAD)) {
       const unsigned long long ci = PHYS ? 0ull : (unsigned long long)__double_as_longlong(B.wc[k].w);
       // visits of a neighbour in the same reference cell (most pairs at a 1 m
       // cell): a constant, without the 27-cell walk of ref_visits
@@ -1151,7 +1152,7 @@ __global__ void __launch_bounds__(256, 4) k_contact_filter(StepParams P) {
       }
       // wall candidates: the triangles of its triangle-grid cell that pass
       // the FP32 pretest, counted here and listed once the arena is reserved
-      if (P.ntri > 0 && tri_cell_range(P, xif, ts, te)) {
+      if (P.ntri > 0 && !(P.wall_far_ok && (flk & PF_WALLFAR)) && tri_cell_range(P, xif, ts, te)) {
         gi = P.ngroups > 1 ? B.grp[k] : 0u;
         for (uint32_t t = ts; t < te; ++t) nw += wall_pretest(P.tri[P.titems[t]], gi, xif, Xi) ? 1u : 0u;
       }
@@ -1447,6 +1448,36 @@ __device__ __forceinline__ bool tri_cell_nonempty(const StepParams& P, float4 xf
   return tri_cell_range(P, xf, s, e) && e > s;
 }
 
+// Whether no triangle can come within reach of a particle at xf (its
+// position at a list rebuild) before the next rebuild: until then it moves
+// less than half the skin, which is less than a triangle-grid cell
+// (wall_far_ok), so its cell stays among the 27 around the present one, and
+// all of those list no triangle; nor can it wrap across a periodic face,
+// which moves it to another part of the mesh.
+__device__ bool wall_far(const StepParams& P, float4 xf) {
+  const float p[3] = {xf.x, xf.y, xf.z};
+  float q[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    if (P.periodic[a]) {
+      const float lo = (float)P.bmin[a], hi = (float)P.bmax[a];
+      if (!(p[a] - lo > P.wall_far_gap && hi - p[a] > P.wall_far_gap)) return false;
+    }
+    q[a] = floorf((p[a] - P.tminf[a]) * P.tinvf);
+    if (!(q[a] == q[a])) return false;  // NaN
+    if (q[a] + 1.0f < 0.0f || q[a] - 1.0f >= (float)P.tdims[a]) return true;  // the 27 cells lie outside the grid
+  }
+  for (int dz = -1; dz <= 1; ++dz)
+    for (int dy = -1; dy <= 1; ++dy)
+      for (int dx = -1; dx <= 1; ++dx) {
+        const int cx = (int)q[0] + dx, cy = (int)q[1] + dy, cz = (int)q[2] + dz;
+        if (cx < 0 || cy < 0 || cz < 0 || cx >= P.tdims[0] || cy >= P.tdims[1] || cz >= P.tdims[2]) continue;
+        const uint32_t cell = (uint32_t)cx + (uint32_t)P.tdims[0] * ((uint32_t)cy + (uint32_t)P.tdims[1] * (uint32_t)cz);
+        if (P.tstart[cell + 1] > P.tstart[cell]) return false;
+      }
+  return true;
+}
+
 // The visiting order of k_accumulate, at a list rebuild: within each tile of
 // 256 slots a counting sort by (triangles listed in the triangle-grid cell,
 // Verlet-list length), dead slots after the live ones. Reads the bank the
@@ -1463,11 +1494,15 @@ __global__ void __launch_bounds__(ACC_TILE) k_accum_order(StepParams P) {
     // keys: 0..62 no triangles, 63 dead, 64..126 triangles, 127 past the end
     uint32_t key = ACC_BINS - 1;
     if (k0 < P.n) {
-      if (B.flags[k0] & PF_DEAD) {
+      const uint32_t fl = B.flags[k0];
+      if (fl & PF_DEAD) {
         key = 63;
       } else {
         key = min(B.ncnt[k0], 62u);
-        if (P.ntri > 0 && tri_cell_nonempty(P, B.xf[k0])) key += 64;
+        const float4 xf = B.xf[k0];
+        if (P.ntri > 0 && tri_cell_nonempty(P, xf)) key += 64;
+        const bool far = P.ntri > 0 && P.wall_far_ok && wall_far(P, xf);
+        B.flags[k0] = far ? (fl | PF_WALLFAR) : (fl & ~PF_WALLFAR);
       }
     }
     for (uint32_t i = threadIdx.x; i < ACC_BINS; i += blockDim.x) bins[i] = 0;

@@ -19,7 +19,9 @@ struct alignas(32) D4 {
   double x, y, z, w;
 };
 
-enum : uint32_t { PF_FIXED = 1u, PF_DEAD = 2u };
+// PF_WALLFAR (set at each list rebuild, with wall_far_ok): no triangle within
+// reach of the slot until the next rebuild, so the filter skips its walls
+enum : uint32_t { PF_FIXED = 1u, PF_DEAD = 2u, PF_WALLFAR = 4u };
 
 enum : unsigned { ST_OVERLAP = 1u, ST_NAN = 2u, ST_NLIST_GROW = 4u, ST_WALL_GROW = 8u };
 
@@ -182,6 +184,8 @@ struct StepParams {
   const uint32_t* tstart;
   const uint32_t* titems;
   const WallMotion* motions;
+  int wall_far_ok;       // the triangle-grid cell exceeds half the skin: PF_WALLFAR is set and read
+  float wall_far_gap;    // half the skin with margin: the distance a slot keeps from a periodic face
   // JKR solver for particle pairs: 0 the reference's Newton, 1 certificates +
   // network + polish, 2 certificates + FP32 Newton from the reference's start
   int jkr_solver;

@@ -216,6 +216,60 @@ def test_wall_candidates_outgrow_their_buffer(rp, oracle_mod):
     assert np.all(Fo[:, 1] > 0)
 
 
+def test_walls_approached_from_afar(rp, oracle_mod):
+    # spheres falling at 10 m/s onto a floor of 4 mm triangles from 12-30 mm
+    # above it, the outer columns drifting across the periodic x faces, with a
+    # 1 mm Verlet skin: a sphere whose neighbourhood held no triangle at a list
+    # rebuild skips its wall pretests until the next one; every step matches
+    # the oracle while the spheres arrive (src/simulation.rs:464-523)
+    lo, hi = (-0.1, -0.05, -0.1), (0.1, 0.1, 0.1)
+    m = 50
+    xs = np.linspace(-0.1, 0.1, m + 1)
+    v = []
+    for i in range(m):
+        for j in range(m):
+            a, b, c, d = (xs[i], 0, xs[j]), (xs[i + 1], 0, xs[j]), (xs[i], 0, xs[j + 1]), (xs[i + 1], 0, xs[j + 1])
+            v += [a + c + b, b + c + d]
+    v = np.array(v, np.float32).astype(np.float64)
+    n = np.tile([0.0, 1.0, 0.0], (len(v), 1))
+    rng = np.random.default_rng(47)
+    gr = np.stack(np.meshgrid(np.arange(6), np.arange(6), indexing="ij"), -1).reshape(-1, 2)
+    k = len(gr)
+    r = rng.uniform(0.004, 0.006, k)
+    x = np.stack([-0.0985 + gr[:, 0] * 0.0394, r + rng.uniform(0.012, 0.03, k), -0.08 + gr[:, 1] * 0.032], 1)
+    vel = np.zeros((k, 3))
+    vel[:, 1] = -10.0
+    vel[:, 0] = np.where(gr[:, 0] == 0, -3.0, np.where(gr[:, 0] == 5, 3.0, 0.0))  # the outer columns wrap
+    vel[:, 2] = rng.normal(0, 0.1, k)
+    st = {"position": x, "radius": r, "mass": 2500.0 * 4.0 / 3.0 * np.pi * r ** 3, "velocity": vel,
+          "angular_velocity": rng.normal(0, 1.0, (k, 3)), "acceleration": np.zeros((k, 3)),
+          "torque": np.zeros((k, 3)), "fixed": np.zeros(k, np.uint8)}
+    wall = (1e8, 0.25, 7800.0, 0.3, 0.6, 0.0)
+    dt = 1e-5
+    per = (True, False, True)
+    o = pu.oracle_sim(oracle_mod, st, dt, lo, hi, 1, 0, per, tris=(v, n), cell=0.02, wall=wall)
+    g = pu.gpu_sim(rp, st, dt, lo, hi, 1, 0, per, tris=(v, n), cell=0.02, wall=wall)
+    g.set_skin(1e-3)
+    touched = np.zeros(k, bool)
+    for step in range(340):
+        o.step()
+        g.step()
+        so, sg = o.state(), g.get_state()
+        assert float(np.max(np.abs(sg["position"] - so["x"]))) < 1e-12, step
+        Fo, To = o.last_forces()
+        Fg, Tg = g.debug_forces()
+        FS, TS = o.last_force_scale()
+        m_ = FS > 0
+        touched |= m_
+        if np.any(m_):
+            assert float((np.linalg.norm(Fg - Fo, axis=1)[m_] / FS[m_]).max()) <= 1e-9, step
+            assert float((np.linalg.norm(Tg - To, axis=1)[m_] / TS[m_]).max()) <= 1e-9, step
+        assert np.array_equal(Fg[~m_], Fo[~m_]) and np.array_equal(Tg[~m_], To[~m_])
+    assert np.count_nonzero(touched) == k  # every sphere reached the floor
+    assert np.all(so["x"][gr[:, 0] == 0, 0] > 0.05)  # the left column wrapped to the right face
+    assert g.stats()["neighbor_rebuilds"] >= 30
+
+
 def test_walls_across_list_rebuilds(rp, oracle_mod):
     # spheres sliding at 0.5 m/s over a floor of 4 mm triangles with a small
     # Verlet skin: the lists are rebuilt every few steps while the wall
