@@ -132,6 +132,11 @@ def hopper_workload(n=1_048_576, seed=2026, phi=0.55):
     fv, fn = floor_triangles(lo, hi)
     return {
         "name": "hopper-1M", "settle": 2000,
+        # Verlet skin of the neighbour lists (a margin of this engine, not of the
+        # reference's algorithm; results do not depend on it): 0.4 mm measured
+        # fastest on this bed over 0.3-0.8 mm (the default, 0.2 of the largest
+        # radius, would be 0.8 mm)
+        "skin": 4e-4,
         "lo": lo, "hi": hi, "periodic": (True, False, True),
         "dt": 2e-6, "normal": "hertz", "tangential": "mindlin",
         "material": (1e7, 0.3, rho, 0.5, 0.5, 0.0),
@@ -354,7 +359,18 @@ def make_sim(rp, wl, mode="parity", precision="fp64"):
             s.set_group_material(g, *m)
     if "velocity" in wl:
         s.set_state({"velocity": wl["velocity"]})
+    if wl.get("skin"):
+        s.set_skin(wl["skin"])
     return s
+
+
+def skin_of(wl, args):
+    """The Verlet skin a timed simulation of `wl` runs with."""
+    if getattr(args, "skin", None):
+        return float(args.skin)
+    if wl.get("skin"):
+        return float(wl["skin"])
+    return 0.2 * float(np.max(wl["radius"]))
 
 
 def one_box_workload(wl, b):
@@ -843,6 +859,8 @@ def run_form(rp, wl, args, dist, device, log, *, mode="parity", precision="fp64"
     steps = steps or args.steps
     warmup = max(3, warmup if warmup is not None else args.warmup)
     sim = make_sim(rp, wl if state is None else wl_at(wl, state), mode, precision)
+    if getattr(args, "skin", None):
+        sim.set_skin(args.skin)
     sim._L.rp_enable_gpu(sim._h, device)
     if host_loop:
         sim._L.rp_set_device_loop(sim._h, 0)
@@ -864,7 +882,8 @@ def run_form(rp, wl, args, dist, device, log, *, mode="parity", precision="fp64"
     res = {"value": value, "unit": UNIT, "ms_per_step": t_max / steps, "steps": steps, "warmup": warmup,
            "particles": int(n_now), "mode": mode, "precision": precision, "wall_s_timed": wall,
            "gpu_launches": int(s1["kernel_launches"] - s0["kernel_launches"]), "clocks": ck,
-           "stats": {k: s1[k] for k in ("neighbor_rebuilds", "max_neighbors", "neighbor_capacity", "removed")}}
+           "stats": {k: s1[k] for k in ("neighbor_rebuilds", "max_neighbors", "neighbor_capacity", "removed")},
+           "verlet_skin_m": skin_of(wl, args)}
     if jkr:
         c1 = sim.jkr_counters()
         d = {k: (c1[k] - c0[k]) / steps for k in c1}
@@ -908,7 +927,8 @@ def jkr_network(rp, wl, state, log):
 
 
 def form_entry(res, force_err=None, extra=None):
-    e = {k: res[k] for k in ("value", "ms_per_step", "particles", "mode", "precision", "clocks", "gpu_launches", "bed")}
+    e = {k: res[k] for k in ("value", "ms_per_step", "particles", "mode", "precision", "clocks", "gpu_launches", "bed",
+                             "verlet_skin_m")}
     e["e2e"] = {"value": res["e2e"]["value"], "wall_ms": res["e2e"]["wall_ms"],
                 "h2d_bytes_per_step": res["e2e"]["h2d_bytes_per_step"],
                 "d2h_bytes_per_step": res["e2e"]["d2h_bytes_per_step"]}
@@ -1189,7 +1209,7 @@ def run_ours(args, log):
         "roofline": res["roofline"], "cpu_baseline": cpu, "cpu_baseline_literal": cpu_lit,
         "e2e": res["e2e"], "gpu_launches": res["gpu_launches"], "clocks": res["clocks"],
         "force_err": ferr, "precision": args.precision, "wall_s_timed": res["wall_s_timed"],
-        "stats": res["stats"], "bed": res.get("bed"),
+        "stats": res["stats"], "verlet_skin_m": res["verlet_skin_m"], "bed": res.get("bed"),
     }
     if "jkr" in res:
         line["jkr"] = res["jkr"]
@@ -1236,6 +1256,8 @@ def main():
     ap.add_argument("--state-in", default=None, help="settled state (.npz from --state-out) instead of relaxing")
     ap.add_argument("--state-out", default=None, help="save the settled state (.npz) before the warm-up")
     ap.add_argument("--host-loop", action="store_true", help="host-issued kernels instead of the device loop")
+    ap.add_argument("--skin", type=float, default=None,
+                    help="Verlet skin in m for the timed simulations (default: 0.2 of the largest radius)")
     ap.add_argument("--profile-only", action="store_true", help="warm-up + timed steps only (for ncu)")
     args = ap.parse_args()
     log = (lambda m: print(m, file=sys.stderr, flush=True))
