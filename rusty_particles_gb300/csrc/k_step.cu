@@ -1055,7 +1055,7 @@ __device__ __forceinline__ uint32_t warp_reserve(uint32_t* ctr, uint32_t v) {
 }
 
 // The contact pass's counters (records, evaluating records, network queue,
-// deferred pairs, wall queue) start every force pass at zero.
+// deferred pairs, wall candidates) start every force pass at zero.
 constexpr int CTOT_WORDS = 8;
 
 // Pass 1 (FP32 and integer work only): the candidates of each particle, i.e.

@@ -143,7 +143,7 @@ struct StepParams {
   uint32_t wcap;    // wall candidate capacity
   uint32_t* coff;   // first result slot of particle k (its ccnt results are contiguous)
   uint32_t* clist;  // compact list of evaluating record slots
-  uint32_t* ctot;   // [0] records, [1] evaluating records, [2] network queue, [3] deferred pairs, [4] wall queue
+  uint32_t* ctot;   // [0] records, [1] evaluating records, [2] network queue, [3] deferred pairs, [4] wall candidates
   uint32_t* jfb;    // evaluating indices deferred to the reference-Newton pass (null: no deferral)
   double* cres;     // per record: force (3) and torque (3) on the row's particle
   float* cresf;     // the same buffer as FP32 records (the mixed form: its pair forces are FP32 values)
