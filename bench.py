@@ -1072,9 +1072,9 @@ def cpu_baselines(wl, state, cache, threads, budget_s, log):
 
 
 # -------------------------------------------------------------------- arms
-def common_config(wl, ws):
+def common_config(wl, ws, mode="parity"):
     n = len(wl["radius"])
-    return {"workload": wl["name"], "describe": wl["describe"], "particles": int(n), "mode": "parity",
+    return {"workload": wl["name"], "describe": wl["describe"], "particles": int(n), "mode": mode,
             "parallelism": f"replicas x{ws}",
             "l2": f"inputs larger than L2 (particle state {n * 312 / 1e6:.0f} MB)"}
 
@@ -1205,7 +1205,7 @@ def run_ours(args, log):
         "metric": METRIC, "value": res["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": res["ms_per_step"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32-pairs/f64-state",
-        "data": "synthetic", "config": common_config(wl, ws),
+        "data": "synthetic", "config": common_config(wl, ws, args.mode),
         "roofline": res["roofline"], "cpu_baseline": cpu, "cpu_baseline_literal": cpu_lit,
         "e2e": res["e2e"], "gpu_launches": res["gpu_launches"], "clocks": res["clocks"],
         "force_err": ferr, "precision": args.precision, "wall_s_timed": res["wall_s_timed"],

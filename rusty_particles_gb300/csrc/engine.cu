@@ -116,7 +116,7 @@ void Engine::free_device() {
     Bank& B = bank_[b];
     dfree(B.xr); dfree(B.vm); dfree(B.wc); dfree(B.acc); dfree(B.tq);
     dfree(B.xres); dfree(B.vres); dfree(B.wres); dfree(B.flags); dfree(B.tag); dfree(B.xref); dfree(B.xf);
-    dfree(B.grp);
+    dfree(B.grp); dfree(B.hmask);
     dfree(B.nbr); dfree(B.ncnt); dfree(B.hist);
   }
   dfree(rb_.ka); dfree(rb_.va); dfree(rb_.kb); dfree(rb_.vb); dfree(rb_.hist); dfree(rb_.part);
@@ -315,7 +315,7 @@ int Engine::alloc_slots(size_t n) {
     TRY(dalloc(&B.xr, na)); TRY(dalloc(&B.vm, na)); TRY(dalloc(&B.wc, na)); TRY(dalloc(&B.acc, na));
     TRY(dalloc(&B.tq, na)); TRY(dalloc(&B.xres, na)); TRY(dalloc(&B.vres, na)); TRY(dalloc(&B.wres, na));
     TRY(dalloc(&B.flags, na)); TRY(dalloc(&B.tag, na)); TRY(dalloc(&B.xref, na)); TRY(dalloc(&B.ncnt, na));
-    TRY(dalloc(&B.xf, na)); TRY(dalloc(&B.grp, na));
+    TRY(dalloc(&B.xf, na)); TRY(dalloc(&B.grp, na)); TRY(dalloc(&B.hmask, na));
   }
   TRY(dalloc(&rb_.ka, na)); TRY(dalloc(&rb_.va, na)); TRY(dalloc(&rb_.kb, na)); TRY(dalloc(&rb_.vb, na));
   TRY(dalloc(&kraw_, na));
@@ -868,7 +868,10 @@ int Engine::upload() {
   }
   for (int b = 0; b < 2; ++b) CK(cudaMemset(bank_[b].ncnt, 0, sizeof(uint32_t) * n_alloc_));
   if (need_hist)
-    for (int b = 0; b < 2; ++b) CK(cudaMemset(bank_[b].hist, 0, sizeof(double) * 3 * n_alloc_ * (size_t)cap_));
+    for (int b = 0; b < 2; ++b) {
+      CK(cudaMemset(bank_[b].hist, 0, sizeof(double) * 3 * n_alloc_ * (size_t)cap_));
+      CK(cudaMemset(bank_[b].hmask, 0, sizeof(unsigned long long) * n_alloc_));
+    }
   TRY(build_params());
   Ctrl c;
   std::memset(&c, 0, sizeof(c));

@@ -384,6 +384,7 @@ __global__ void k_build_nlist(StepParams P, const uint32_t* cstart, const uint32
       }
     }
     uint32_t cnt = 0;
+    unsigned long long hm = 0ull;  // springs carried over with a value other than +0
     const uint32_t ok = carry_history ? perm[k] : 0u;
     const uint32_t ocnt = carry_history ? O.ncnt[ok] : 0u;
     const uint32_t* orow = O.nbr + (size_t)ok * P.cap;
@@ -430,6 +431,8 @@ __global__ void k_build_nlist(StepParams P, const uint32_t* cstart, const uint32
                   B.hist[ni] = h0;
                   B.hist[plane_new + ni] = h1;
                   B.hist[2 * plane_new + ni] = h2;
+                  if (cnt < 64 && (__double_as_longlong(h0) | __double_as_longlong(h1) | __double_as_longlong(h2)))
+                    hm |= 1ull << cnt;
                 }
               }
               ++cnt;
@@ -437,6 +440,7 @@ __global__ void k_build_nlist(StepParams P, const uint32_t* cstart, const uint32
           }
         }
     B.ncnt[k] = cnt < (uint32_t)P.cap ? cnt : (uint32_t)P.cap;
+    if (carry_history) B.hmask[k] = hm;
     atomicMax(&P.ctrl->max_count, cnt);
     if (cnt > (uint32_t)P.cap) atomicOr(&P.ctrl->halt, HALT_LISTS);
   }

@@ -1107,6 +1107,8 @@ __global__ void __launch_bounds__(256, 4) k_contact_filter(StepParams P) {
       const uint32_t cnt = B.ncnt[k];
       const uint32_t* row = B.nbr + (size_t)k * P.cap;
       CRec* out = P.crec + (size_t)k * P.cap;
+      unsigned long long hm = HIST ? B.hmask[k] : 0ull;
+      const unsigned long long hm0 = hm;
       // the next entry and its FP32 position are loaded while this one is
       // tested (rows and positions are read-only during the pass)
       uint32_t jn = cnt > 0 ? __ldg(row) : 0u;
@@ -1142,14 +1144,17 @@ __global__ void __launch_bounds__(256, 4) k_contact_filter(StepParams P) {
           if (evaluates) ++ncmp;
           if (net) ++nnet;
         } else {
-          if (HIST) {
+          // a spring out of reach resets; one already +0 (its bit clear) stays
+          if (HIST && (m >= 64 || ((hm >> m) & 1ull))) {
             B.hist[hi] = 0.0;
             B.hist[plane + hi] = 0.0;
             B.hist[2 * plane + hi] = 0.0;
+            if (m < 64) hm &= ~(1ull << m);
           }
           if (P.debug) P.dbgMult[hi] = 0;
         }
       }
+      if (HIST && hm != hm0) B.hmask[k] = hm;
       // wall candidates: the triangles of its triangle-grid cell that pass
       // the FP32 pretest, counted here and listed once the arena is reserved
       if (P.ntri > 0 && !(P.wall_far_ok && (flk & PF_WALLFAR)) && tri_cell_range(P, xif, ts, te)) {
@@ -1332,6 +1337,7 @@ __device__ __forceinline__ bool contact_eval(const StepParams& P, const Bank& B,
       nrm = cvt<R>(nd);
     }
     if (deferred) return true;
+    if (HIST && m < 64) atomicOr(B.hmask + k, 1ull << m);
   } else if (HIST) {
     hk[0] = 0.0;
     hk[plane] = 0.0;
@@ -1352,6 +1358,8 @@ __device__ __forceinline__ bool contact_eval(const StepParams& P, const Bank& B,
         B.hist[h2] = -hk[0];
         B.hist[plane + h2] = -hk[plane];
         B.hist[2 * plane + h2] = -hk[2 * plane];
+        const uint32_t m2 = rj[c2].mv & 0xFFFFu;
+        if (m2 < 64) atomicOr(B.hmask + j, 1ull << m2);
       }
       if (P.debug) P.dbgMult[h2] = (uint8_t)(in ? vji : 0);
       break;

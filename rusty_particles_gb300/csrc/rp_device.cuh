@@ -95,6 +95,9 @@ struct Bank {
   uint32_t* nbr;    // neighbour rows, cap entries per slot
   uint32_t* ncnt;   // row lengths
   double* hist;     // physical-mode tangential spring per row entry: 3 planes of N*cap
+  // physical mode: bit m set when the spring of row entry m (< 64) may hold a
+  // value other than +0 (entries past 64 are always treated as live)
+  unsigned long long* hmask;
   uint32_t* grp;    // group (independent bed) of the slot
 };
 
