@@ -827,6 +827,7 @@ __global__ void __launch_bounds__(128) k_force(StepParams P) {
     V F = vmk(0.0, 0.0, 0.0), T = vmk(0.0, 0.0, 0.0);
     const uint32_t cnt = B.ncnt[k];
     const uint32_t* row = B.nbr + (size_t)k * P.cap;
+    unsigned long long hm = 0ull;  // springs this row writes (the live-spring mask)
     const float4 xif = B.xf[k];
     const float Xi = fmaxf(fmaxf(fabsf(xif.x), fabsf(xif.y)), fabsf(xif.z));
     for (uint32_t m = 0; m < cnt; ++m) {
@@ -886,6 +887,7 @@ __global__ void __launch_bounds__(128) k_force(StepParams P) {
             pair_contact<double, PHYS, HIST>(P, lw, d, d2, rsum, ri, rj, mi, vj4.w, vi, xyz(vj4), wi, xyz(wj4),
                                              HIST ? B.hist + hi : nullptr, plane, fc, tc, nrm, excess);
           }
+          if (HIST && m < 64) hm |= 1ull << m;
           for (int t = 0; t < visits; ++t) {
             F = F + fc;
             T = T + tc;
@@ -899,6 +901,7 @@ __global__ void __launch_bounds__(128) k_force(StepParams P) {
       }
       if (P.debug) P.dbgMult[hi] = (uint8_t)visits;
     }
+    if (HIST && hm) B.hmask[k] |= hm;
     wall_forces(P, lw, gi, xi, xif, vi, wi, ri, mi, F, T, excess);
     if (P.debug) {
       P.dbgF[3 * (size_t)k] = F.x; P.dbgF[3 * (size_t)k + 1] = F.y; P.dbgF[3 * (size_t)k + 2] = F.z;

@@ -68,3 +68,4 @@ def test_springs_survive_rebuilds(rp, oracle_mod, tangential):
     assert rebuilds >= 20, rebuilds
     assert loaded > 500, loaded
     print(f"\n{rebuilds} rebuilds in 60 steps, worst force error {worst_f:.2e}, worst position error {worst_x:.2e}")
+
