@@ -1112,16 +1112,19 @@ __global__ void __launch_bounds__(256, 4) k_contact_filter(StepParams P) {
       CRec* out = P.crec + (size_t)k * P.cap;
       unsigned long long hm = HIST ? B.hmask[k] : 0ull;
       const unsigned long long hm0 = hm;
-      // the next entry and its FP32 position are loaded while this one is
-      // tested (rows and positions are read-only during the pass)
-      uint32_t jn = cnt > 0 ? __ldg(row) : 0u;
+      // the next two entries and their FP32 positions are loaded while this
+      // one is tested (rows and positions are read-only during the pass)
+      uint32_t jn = cnt > 0 ? __ldg(row) : 0u, jn2 = cnt > 1 ? __ldg(row + 1) : 0u;
       float4 xn = cnt > 0 ? __ldg(B.xf + jn) : make_float4(0.f, 0.f, 0.f, 0.f);
+      float4 xn2 = cnt > 1 ? __ldg(B.xf + jn2) : make_float4(0.f, 0.f, 0.f, 0.f);
       for (uint32_t m = 0; m < cnt; ++m) {
         const uint32_t j = jn;
         const float4 xjf = xn;
-        if (m + 1 < cnt) {
-          jn = __ldg(row + m + 1);
-          xn = __ldg(B.xf + jn);
+        jn = jn2;
+        xn = xn2;
+        if (m + 2 < cnt) {
+          jn2 = __ldg(row + m + 2);
+          xn2 = __ldg(B.xf + jn2);
         }
         const size_t hi = (size_t)k * P.cap + m;
         int vij = 0, vji = 0;
