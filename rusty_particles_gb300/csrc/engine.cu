@@ -1544,8 +1544,8 @@ int Engine::stats(rp_stats* s) {
   return RP_OK;
 }
 
-// Bed statistics of the current state (the reference's scripts and SURVEY's
-// long-run checks use these three): kinetic energy, coordination number (2 x
+// Bed statistics of the current state (the reference's scripts and the
+// long-run statistical checks use these three): kinetic energy, coordination number (2 x
 // overlapping pairs / particles) and the spheres' volume over the box's.
 int Engine::bed_statistics(double out[3]) {
   TRY(ensure_gpu());
