@@ -1764,8 +1764,10 @@ void launch_bed_stats(const StepParams& P, double* out, unsigned long long* pair
 
 int launch_first_half(const StepParams& P, cudaStream_t s) {
   if (P.n == 0) return 0;
+  // the Kahan form holds 90 registers: blocks of 128 keep 20 warps resident
+  // per multiprocessor where blocks of 256 keep 16
   if (P.prec == 1) k_first_half<false><<<grid_for(P.n, 256), 256, 0, s>>>(P);
-  else k_first_half<true><<<grid_for(P.n, 256), 256, 0, s>>>(P);
+  else k_first_half<true><<<grid_for(P.n, 128), 128, 0, s>>>(P);
   return 1;
 }
 
