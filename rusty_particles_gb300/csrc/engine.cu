@@ -484,6 +484,19 @@ int Engine::build_params() {
     }
     P.gravity[k] = gravity[k];
   }
+  {
+    // the FP32 mirror of a position is within 2^-24 |x| of it: a margin of
+    // 1e-6 (|bounds| + 2) keeps the inner intervals inside the exact ones
+    double bmag = 0.0;
+    for (int k = 0; k < 3; ++k) bmag = std::max(bmag, std::max(std::fabs(bmin[k]), std::fabs(bmax[k])));
+    const double m = 1e-6 * (bmag + 2.0);
+    for (int k = 0; k < 3; ++k) {
+      const double lo = periodic[k] ? bmin[k] + m : bmin[k] - 1.0 + m;
+      const double hi = periodic[k] ? bmax[k] - m : (k == 1 ? INFINITY : bmax[k] + 1.0 - m);
+      P.inner_lo[k] = std::nextafter((float)lo, INFINITY);
+      P.inner_hi[k] = std::isinf(hi) ? INFINITY : std::nextafter((float)hi, -INFINITY);
+    }
+  }
   P.pm = pm;
   P.wm = wm;
   // per-group law constants (group 0: the particle material)

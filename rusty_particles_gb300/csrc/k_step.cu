@@ -593,14 +593,21 @@ __global__ void __launch_bounds__(256) k_first_half(StepParams P) {
         kahan_add(w, wres, dw);
       }
     }
+    // the FP32 mirror of x (written with it) decides most wrap and removal
+    // tests without the FP64 comparisons: inside the inner interval of an
+    // axis, x needs no wrap (periodic) or is kept (open)
+    const float4 xo = B.xf[k];
+    const bool in0 = xo.x > P.inner_lo[0] && xo.x < P.inner_hi[0];
+    const bool in1 = xo.y > P.inner_lo[1] && xo.y < P.inner_hi[1];
+    const bool in2 = xo.z > P.inner_lo[2] && xo.z < P.inner_hi[2];
     if (anyp) {
-      if (P.periodic[0]) { if (x.x < P.bmin[0]) x.x = x.x + P.bsize[0]; else if (x.x >= P.bmax[0]) x.x = x.x - P.bsize[0]; }
-      if (P.periodic[1]) { if (x.y < P.bmin[1]) x.y = x.y + P.bsize[1]; else if (x.y >= P.bmax[1]) x.y = x.y - P.bsize[1]; }
-      if (P.periodic[2]) { if (x.z < P.bmin[2]) x.z = x.z + P.bsize[2]; else if (x.z >= P.bmax[2]) x.z = x.z - P.bsize[2]; }
+      if (P.periodic[0] && !in0) { if (x.x < P.bmin[0]) x.x = x.x + P.bsize[0]; else if (x.x >= P.bmax[0]) x.x = x.x - P.bsize[0]; }
+      if (P.periodic[1] && !in1) { if (x.y < P.bmin[1]) x.y = x.y + P.bsize[1]; else if (x.y >= P.bmax[1]) x.y = x.y - P.bsize[1]; }
+      if (P.periodic[2] && !in2) { if (x.z < P.bmin[2]) x.z = x.z + P.bsize[2]; else if (x.z >= P.bmax[2]) x.z = x.z - P.bsize[2]; }
     }
-    bool keep = (P.periodic[0] || (x.x >= P.bmin[0] - 1.0 && x.x <= P.bmax[0] + 1.0)) &&
-                (P.periodic[1] || (x.y >= P.bmin[1] - 1.0)) &&
-                (P.periodic[2] || (x.z >= P.bmin[2] - 1.0 && x.z <= P.bmax[2] + 1.0));
+    bool keep = (P.periodic[0] || in0 || (x.x >= P.bmin[0] - 1.0 && x.x <= P.bmax[0] + 1.0)) &&
+                (P.periodic[1] || in1 || (x.y >= P.bmin[1] - 1.0)) &&
+                (P.periodic[2] || in2 || (x.z >= P.bmin[2] - 1.0 && x.z <= P.bmax[2] + 1.0));
     if (!keep) {
       B.flags[k] = fl | PF_DEAD;
       const double nan = __longlong_as_double(0x7ff8000000000000ll);

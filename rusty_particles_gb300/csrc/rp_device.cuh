@@ -156,6 +156,9 @@ struct StepParams {
   double dt;
   double bmin[3], bmax[3], bsize[3];
   float bsizef[3];  // (float)bsize: FP32 kernels take no double-to-float conversion per use
+  // per axis, an FP32 interval whose interior (on the FP32 mirror) proves the
+  // FP64 position needs no periodic wrap (periodic axes) or is kept (open axes)
+  float inner_lo[3], inner_hi[3];
   uint32_t bq_hi[3]; // high word of the bits of bsize/4: |d| has a smaller high word => |d| < bsize/4
   double gravity[3];
   Material pm, wm;
